@@ -1,0 +1,72 @@
+"""Shared drivers that call an EmDee-ABI library the way the reference's
+test programs do (test/common/contained.f90:58-87)."""
+import ctypes as C
+import json
+import os
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def load_golden(name):
+    with open(os.path.join(GOLDEN, name)) as f:
+        return json.load(f)
+
+
+def setup_lj_sample(lib, cfg, modifier="none", skin_width=None, threads=2, precision=None):
+    """test/test_pair_lj_*.f90:33-44 on the NIST LJ sample."""
+    run = cfg["run"]
+    N = len(cfg["coordinates"])
+    md = lib.system(threads, 1, run["Rc"], run["skin"], N, cfg["type"], cfg["mass"])
+    if precision is not None:
+        lib.EmDee_set_precision(md, precision)
+    for i, (eps, sig) in enumerate(zip(cfg["epsilon"], cfg["sigma"])):
+        p = lib.EmDee_pair_lj_cut(eps / run["mvv2e"], sig)
+        if modifier == "shifted_force":
+            p = lib.EmDee_shifted_force(p)
+        elif modifier == "square_smoothed":
+            p = lib.EmDee_square_smoothed(p, skin_width)
+        elif modifier == "shifted_square_smoothed":
+            p = lib.EmDee_shifted_square_smoothed(p, skin_width)
+        lib.EmDee_set_pair_model(md, i + 1, i + 1, p, run["kCoul"])
+    return md
+
+
+def initialize(lib, md, cfg, seed=None, kT=None):
+    run = cfg["run"]
+    lib.upload(md, "charges", cfg["charge"])
+    lib.upload(md, "box", np.array([cfg["box"]]))
+    lib.upload(md, "coordinates", np.array(cfg["coordinates"]))
+    lib.EmDee_random_momenta(C.byref(md), run["kB"] * run["temp"] if kT is None else kT, True,
+                             run["seed"] if seed is None else seed)
+
+
+def velocity_verlet(lib, md, dt, nsteps, nprop=1, on_step=None):
+    """test/common/contained.f90:63-72"""
+    for step in range(1, nsteps + 1):
+        md.Options.Compute = (step % nprop == 0)
+        lib.EmDee_boost(C.byref(md), 1.0, 0.0, 0.5 * dt)
+        lib.EmDee_displace(C.byref(md), 1.0, 0.0, dt)
+        lib.EmDee_boost(C.byref(md), 1.0, 0.0, 0.5 * dt)
+        if on_step is not None:
+            on_step(step, md)
+
+
+def observables(md, mvv2e=1.0):
+    return np.array([mvv2e * md.Energy.Potential, mvv2e * md.Virial.Total,
+                     mvv2e * (md.Energy.Potential + md.Kinetic.Total)])
+
+
+def fcc_lattice(N, L, jitter, seed):
+    """fcc sites filling the smallest 4 n^3 lattice >= N (first N sites), jittered
+    uniformly by +-jitter; the box-filling idea of src/testc.c:77-89."""
+    n = 1
+    while 4 * n ** 3 < N:
+        n += 1
+    a = L / n
+    base = np.array([[0, 0, 0], [0.5, 0.5, 0], [0.5, 0, 0.5], [0, 0.5, 0.5]])
+    g = np.stack(np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij"), -1).reshape(-1, 3)
+    sites = (g[:, None, :] + base[None, :, :]).reshape(-1, 3)[:N] * a
+    rng = np.random.default_rng(seed)
+    return sites + rng.uniform(-jitter, jitter, size=sites.shape)
