@@ -1,0 +1,363 @@
+#!/usr/bin/env python
+"""Throughput of the EmDee hot path on GB300: atom-steps/s of velocity-Verlet MD.
+
+Workload (the 1M-atom Lennard-Jones box): N = 4*64^3 = 1,048,576 atoms on an fcc
+lattice jittered by U(+-0.05 sigma) (seed 86245), reduced density 0.8442
+(L = 107.494), lj_cut with rc = 2.5, neighbor skin 0.3, Maxwell-Boltzmann
+momenta at T* = 1.5 from EmDee_random_momenta, dt = 0.005.  One step is the
+reference's velocity-Verlet loop body (test/common/contained.f90:63-72):
+EmDee_boost(dt/2), EmDee_displace(dt), EmDee_boost(dt/2), energies every 100
+steps, neighbor lists rebuilt whenever the skin check fires.  FP32 pair math,
+FP64 positions, momenta, energy and virial sums.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+`--impl reference` times the reference algorithm's CPU implementation (the
+OpenMP C restatement in oracle/, all host threads) on the same workload.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(name="lj_fcc_1048576", N=4 * 64 ** 3, rho=0.8442, rc=2.5, skin=0.3, kT=1.5, dt=0.005,
+                seed=86245, jitter=0.05, nprop=100)
+METRIC = "atom-steps/s"
+ORACLE_SO = os.path.join(ROOT, "oracle", "_build", "liboracle_emdee.so")
+
+
+def fcc(N, rho, jitter, seed):
+    n = 1
+    while 4 * n ** 3 < N:
+        n += 1
+    L = (N / rho) ** (1.0 / 3.0)
+    a = L / n
+    base = np.array([[0, 0, 0], [0.5, 0.5, 0], [0.5, 0, 0.5], [0, 0.5, 0.5]])
+    g = np.stack(np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij"), -1).reshape(-1, 3)
+    R = (g[:, None, :] + base[None, :, :]).reshape(-1, 3)[:N] * a
+    R += np.random.default_rng(seed).uniform(-jitter, jitter, size=R.shape)
+    return np.ascontiguousarray(R), L
+
+
+def setup(lib, W, threads=1, precision=None):
+    R, L = fcc(W["N"], W["rho"], W["jitter"], W["seed"])
+    md = lib.system(threads, 1, W["rc"], W["skin"], W["N"])
+    if precision is not None:
+        lib.EmDee_set_precision(md, precision)
+    lib.EmDee_set_pair_model(md, 1, 1, lib.EmDee_pair_lj_cut(1.0, 1.0), 0.0)
+    lib.upload(md, "box", np.array([L]))
+    lib.upload(md, "coordinates", R)
+    lib.EmDee_random_momenta(C.byref(md), W["kT"], True, W["seed"])
+    return md
+
+
+def vv(lib, md, W, nsteps, step0=0, per_step=None):
+    dt = W["dt"]
+    for k in range(nsteps):
+        md.Options.Compute = ((step0 + k + 1) % W["nprop"] == 0)
+        if per_step is not None:
+            per_step[0](md)
+        lib.EmDee_boost(C.byref(md), 1.0, 0.0, 0.5 * dt)
+        lib.EmDee_displace(C.byref(md), 1.0, 0.0, dt)
+        lib.EmDee_boost(C.byref(md), 1.0, 0.0, 0.5 * dt)
+        if per_step is not None:
+            per_step[1](md)
+
+
+# ---------------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------------
+
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.path = tempfile.mktemp(suffix=".csv")
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def fp32_peak_tflops(torch):
+    """Dense FP32 (CUDA-core) throughput measured here: cuBLAS SGEMM 8192^3 with
+    TF32 disabled, best of 5."""
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    n = 8192
+    a = torch.randn(n, n, device="cuda", dtype=torch.float32)
+    b = torch.randn(n, n, device="cuda", dtype=torch.float32)
+    for _ in range(2):
+        a @ b
+    best = 0.0
+    for _ in range(5):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        a @ b
+        e.record()
+        e.synchronize()
+        best = max(best, 2.0 * n ** 3 / (s.elapsed_time(e) * 1e-3) / 1e12)
+    torch.backends.cuda.matmul.allow_tf32 = prev
+    del a, b
+    torch.cuda.empty_cache()
+    return best
+
+
+def read_traffic():
+    """DRAM bytes per pair-kernel launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "pair_lj1m_traffic.txt")
+    try:
+        for line in open(p):
+            if line.startswith("dram_bytes_per_launch"):
+                return float(line.split()[1])
+    except OSError:
+        pass
+    return None
+
+
+# ---------------------------------------------------------------------------------
+# CPU arm (oracle restatement, all host threads)
+# ---------------------------------------------------------------------------------
+
+def cpu_rate(W, budget_s, max_steps, warmup=1):
+    from emdee_gb300.emdee import EmDee
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+    lib = EmDee(ORACLE_SO)
+    threads = os.cpu_count() or 1
+    md = setup(lib, W, threads=threads)
+    vv(lib, md, W, warmup)
+    t0 = time.perf_counter()
+    n = 0
+    while n < max_steps and (time.perf_counter() - t0) < budget_s:
+        vv(lib, md, W, 1, step0=warmup + n)
+        n += 1
+    t = time.perf_counter() - t0
+    return W["N"] * n / t, threads, n, t
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    W = dict(WORKLOAD)
+    rate, threads, n, t = cpu_rate(W, budget_s=150.0, max_steps=args.steps, warmup=min(args.warmup, 1))
+    line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": "atom-steps/s", "n_gpus": args.gpus,
+            "steps": n, "warmup": min(args.warmup, 1), "ms_per_step": 1e3 * t / max(n, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded fcc lattice)",
+            "config": {"workload": W["name"], "N": W["N"], "rho": W["rho"], "rc": W["rc"], "skin": W["skin"],
+                       "dt": W["dt"]},
+            "cpu_baseline": {"value": rate, "unit": "atom-steps/s", "cores": threads, "kind": "port",
+                             "sample": "%d velocity-Verlet steps of the full %d-atom box (%.1f s, capped at 150 s)"
+                                       % (n, W["N"], t)},
+            "e2e": {"value": rate, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------------
+
+def run_gpu(args):
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from emdee_gb300.build import build
+    build()
+    import emdee_gb300
+    lib = emdee_gb300.load()
+    W = dict(WORKLOAD)
+    N = W["N"]
+    md = setup(lib, W, precision=emdee_gb300.MIXED)
+    vv(lib, md, W, args.warmup)
+    stream = torch.cuda.ExternalStream(lib.EmDee_cuda_stream(md))
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    # ---- timed region (device-resident state) ----
+    clocks = Clocks(local)
+    launches0 = lib.EmDee_launch_count(md)
+    barrier()
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    builds0 = md.Builds
+    e0.record(stream)
+    vv(lib, md, W, args.steps, step0=args.warmup)
+    e1.record(stream)
+    e1.synchronize()
+    barrier()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    launches = lib.EmDee_launch_count(md) - launches0
+    builds = md.Builds - builds0
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * N * args.steps / (ms * 1e-3)
+
+    # ---- per-kernel device times (same workload, CUDA events on the library stream) ----
+    lib.EmDee_profile(md, 1)
+    nprof = min(args.steps, 200)
+    vv(lib, md, W, nprof, step0=args.warmup + args.steps)
+    kms = (C.c_double * 6)()
+    kn = (C.c_long * 6)()
+    lib.EmDee_kernel_times(md, kms, kn, 6)
+    lib.EmDee_profile(md, 0)
+    names = ["skin", "build", "pack", "pair", "boost", "move"]
+    per_kernel = {nm: {"launches": int(kn[i]), "ms_total": kms[i],
+                       "us_per_launch": (1e3 * kms[i] / kn[i]) if kn[i] else None} for i, nm in enumerate(names)}
+    listed, within = C.c_long(), C.c_long()
+    lib.EmDee_pair_statistics(md, C.byref(listed), C.byref(within))
+    flops = 8.0 * listed.value + 22.0 * within.value
+    pair_s = kms[3] / kn[3] * 1e-3
+    peaks, peak_kind = measured_peaks()
+    fp32_peak = fp32_peak_tflops(torch)
+    achieved = flops / pair_s / 1e12
+    traffic = read_traffic()
+    roofline = {"bound": "fp32", "kernel": "k_pair_mixed (pair forces)", "achieved": achieved,
+                "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": traffic,
+                "peak_source": "cuBLAS SGEMM 8192^3, TF32 off, measured in this run",
+                "flops_per_launch": flops, "half_list_pairs": listed.value, "pairs_within_rc": within.value,
+                "us_per_launch": pair_s * 1e6}
+    boost_bytes = 72.0 * N   # P read+write, F read
+    move_bytes = 80.0 * N    # R read+write, P read, 1/m read
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    boost_gbs = boost_bytes / (kms[4] / kn[4] * 1e-3) / 1e9 if kn[4] else None
+    move_gbs = move_bytes / (kms[5] / kn[5] * 1e-3) / 1e9 if kn[5] else None
+    roofline_hbm = {"bound": "hbm", "kernel": "k_move (EmDee_displace)", "achieved": move_gbs, "peak": hbm,
+                    "unit": "GB/s", "frac": (move_gbs / hbm) if move_gbs else None, "traffic": None,
+                    "peak_source": peak_kind, "boost_achieved_gbs": boost_gbs}
+
+    # ---- end to end through the C ABI with host buffers ----
+    pin = lambda: torch.empty((N, 3), dtype=torch.float64, pin_memory=True).numpy()
+    Ph, Rh = pin(), pin()
+    lib.EmDee_download(md, b"momenta", Ph.ctypes.data_as(C.c_void_p))
+
+    def pre(m):
+        lib.EmDee_upload(C.byref(m), b"momenta", Ph.ctypes.data_as(C.c_void_p))
+
+    def post(m):
+        lib.EmDee_download(m, b"coordinates", Rh.ctypes.data_as(C.c_void_p))
+        lib.EmDee_download(m, b"momenta", Ph.ctypes.data_as(C.c_void_p))
+
+    ne2e = min(args.steps, 500)
+    barrier()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    vv(lib, md, W, ne2e, step0=0, per_step=(pre, post))
+    f1.record(stream)
+    f1.synchronize()
+    barrier()
+    e2e_ms = f0.elapsed_time(f1)
+    e2e = {"value": world * N * ne2e / (e2e_ms * 1e-3), "unit": "atom-steps/s", "h2d_bytes_per_step": 24 * N,
+           "d2h_bytes_per_step": 48 * N + 40, "steps": ne2e,
+           "per_step": "EmDee_upload(momenta) from pinned host memory, boost/displace/boost, "
+                       "EmDee_download(coordinates) and EmDee_download(momenta) into pinned host memory"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        rate, threads, n, t = cpu_rate(W, budget_s=20.0, max_steps=100)
+        cpu = {"value": rate, "unit": "atom-steps/s", "cores": threads, "kind": "port",
+               "sample": "%d velocity-Verlet steps of the full %d-atom box after 1 warm-up step (%.1f s)"
+                         % (n, N, t)}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "atom-steps/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32 pair math, f64 state",
+                "data": "synthetic (seeded fcc lattice, Maxwell-Boltzmann momenta)",
+                "config": {"workload": W["name"], "N": N, "rho": W["rho"], "L": (N / W["rho"]) ** (1 / 3),
+                           "rc": W["rc"], "skin": W["skin"], "kT": W["kT"], "dt": W["dt"],
+                           "energies_every": W["nprop"], "neighbor_builds_in_timed_region": builds,
+                           "parallelism": "replicas" if world > 1 else "single GPU",
+                           "l2": "no flush; per-step working set (R, P, F, packed positions, lists) ~0.4 GB "
+                                 "> 129 MB L2"},
+                "clocks": clk, "gpu_launches": int(launches), "roofline": roofline, "roofline_hbm": roofline_hbm,
+                "kernels": per_kernel, "e2e": e2e, "cpu_baseline": cpu}
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--atoms", type=int, default=None,
+                    help="smaller box of the same density (profiling runs); default 1,048,576")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.atoms:
+        WORKLOAD["N"] = args.atoms
+        WORKLOAD["name"] = "lj_fcc_%d" % args.atoms
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,152 @@
+// motion.cu -- phase-space updates (src/EmDeeData.f90:823-922) and the force
+// dispatcher.
+//
+// boost:  P <- CP P + CF F, with the per-dimension 2KE = sum P^2/m when energies
+//         are requested (src/EmDeeData.f90:864-922);
+// move:   R <- CR R + CP P/m (src/EmDeeData.f90:823-860).
+// FP64 throughout; compiled with -fmad=false so each update rounds exactly like
+// the reference's statement.
+#include "reduce.cuh"
+#include <vector>
+
+#include "system.hpp"
+
+namespace emdee {
+
+void device_pair_forces_mixed(System& s, bool compute, bool useInRc, double rc2scaled, int variant);
+void device_pair_forces_fp64(System& s, bool compute, bool useInRc, double rc2scaled);
+
+static const int MOTION_THREADS = 256;
+
+// UNITCP: CP == 1, so CP*P == P exactly and is skipped; UNITM: all masses are
+// 1, so multiplications by 1/m are skipped.  Both leave every rounding as in
+// the reference's statements.
+template <bool KIN, bool UNITCP, bool UNITM>
+__global__ void __launch_bounds__(MOTION_THREADS) k_boost(double* __restrict__ P, const double* __restrict__ F,
+                                                          const double* __restrict__ invMass, int N, double CP,
+                                                          double CF, double* partials, unsigned int* ticket,
+                                                          double* result) {
+  double k2[3] = {0.0, 0.0, 0.0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    double im = (KIN && !UNITM) ? invMass[i] : 1.0;
+    for (int d = 0; d < 3; d++) {
+      double p = (UNITCP ? P[3 * i + d] : CP * P[3 * i + d]) + CF * F[3 * i + d];
+      P[3 * i + d] = p;
+      if (KIN) k2[d] += UNITM ? p * p : im * (p * p);
+    }
+  }
+  if (KIN) grid_reduce<3, MOTION_THREADS>(k2, partials, ticket, result + 10);
+}
+
+template <bool UNITCR, bool UNITM>
+__global__ void __launch_bounds__(MOTION_THREADS) k_move(double* __restrict__ R, const double* __restrict__ P,
+                                                         const double* __restrict__ invMass, int N, double CR,
+                                                         double CP) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  double im = UNITM ? 1.0 : invMass[i];
+  for (int d = 0; d < 3; d++) {
+    double dr = UNITM ? CP * P[3 * i + d] : CP * P[3 * i + d] * im;
+    R[3 * i + d] = (UNITCR ? R[3 * i + d] : CR * R[3 * i + d]) + dr;
+  }
+}
+
+static int motion_blocks(int N) {
+  int b = (N + MOTION_THREADS - 1) / MOTION_THREADS;
+  return b < 1184 ? b : 1184;   // 152 SMs x 8 resident blocks, grid-stride beyond
+}
+
+void device_boost(System& s, double CP, double CF, bool kinetic) {
+  int N = s.natoms, blocks = motion_blocks(N);
+  if (kinetic) {
+    if (s.keCap < blocks) {
+      CK(cudaFree(s.dKE));
+      s.keCap = blocks;
+      CK(cudaMalloc(&s.dKE, sizeof(double) * 3 * blocks));
+    }
+    prof_begin(s, PK_BOOST);
+    auto kern = CP == 1.0 ? (s.unitMass ? k_boost<true, true, true> : k_boost<true, true, false>)
+                          : (s.unitMass ? k_boost<true, false, true> : k_boost<true, false, false>);
+    kern<<<blocks, MOTION_THREADS, 0, s.stream>>>(s.dP, s.F(), s.dInvMass, N, CP, CF, s.dKE, s.dTicket + 1,
+                                                  s.dResult);
+    CK(cudaGetLastError());
+    prof_end(s, PK_BOOST);
+    CK(cudaMemcpyAsync(s.hResult + 10, s.dResult + 10, 3 * sizeof(double), cudaMemcpyDeviceToHost, s.stream));
+    CK(cudaStreamSynchronize(s.stream));
+  } else {
+    prof_begin(s, PK_BOOST);
+    auto kern = CP == 1.0 ? k_boost<false, true, true> : k_boost<false, false, true>;
+    kern<<<blocks, MOTION_THREADS, 0, s.stream>>>(s.dP, s.F(), s.dInvMass, N, CP, CF, nullptr, nullptr, nullptr);
+    CK(cudaGetLastError());
+    prof_end(s, PK_BOOST);
+  }
+}
+
+void device_move(System& s, double CR, double CP) {
+  int N = s.natoms;
+  prof_begin(s, PK_MOVE);
+  auto kern = CR == 1.0 ? (s.unitMass ? k_move<true, true> : k_move<true, false>)
+                        : (s.unitMass ? k_move<false, true> : k_move<false, false>);
+  kern<<<(N + MOTION_THREADS - 1) / MOTION_THREADS, MOTION_THREADS, 0, s.stream>>>(s.dR, s.dP, s.dInvMass, N, CR, CP);
+  CK(cudaGetLastError());
+  prof_end(s, PK_MOVE);
+}
+
+// Chooses the force kernel for the current layer and leaves the four sums in
+// hResult[0..3] (src/EmDeeData.f90:644-685).
+void device_pair_forces(System& s, bool compute) {
+  const int l = s.layer - 1;
+  const double L = *s.Lbox, invL2 = 1.0 / (L * L);
+  const bool useInRc = s.useInRc[l] != 0;
+  const double rc2 = (useInRc ? s.InRcSq : s.RcSq) * invL2;   // src/EmDeeData.f90:660-667
+  if (!s.pairs_exist[l]) {
+    CK(cudaMemsetAsync(s.F(), 0, sizeof(double) * 3 * s.natoms, s.stream));
+    CK(cudaStreamSynchronize(s.stream));
+    for (int q = 0; q < 4; q++) s.hResult[q] = 0.0;
+    return;
+  }
+  if (s.partialCap < s.grid.nTiles) {
+    CK(cudaFree(s.dPartials));
+    s.partialCap = s.grid.nTiles;
+    CK(cudaMalloc(&s.dPartials, sizeof(double) * 5 * s.partialCap));
+  }
+  prof_begin(s, PK_PAIR);
+  if (s.precision == 1) {
+    device_pair_forces_fp64(s, compute, useInRc, rc2);
+  } else {
+    // single-type Lennard-Jones without charges takes the specialised kernel
+    bool lj_only = s.ntypes == 1 && s.P(0, 0, l).model.kind == MK_LJ_CUT &&
+                   !(s.P(0, 0, l).coulomb && s.coul[l].kind != MK_COUL_NONE);
+    device_pair_forces_mixed(s, compute, useInRc, rc2, lj_only ? 0 : 1);
+  }
+  prof_end(s, PK_PAIR);
+  CK(cudaMemcpyAsync(s.hResult, s.dResult, 4 * sizeof(double), cudaMemcpyDeviceToHost, s.stream));
+  CK(cudaStreamSynchronize(s.stream));
+}
+
+// Half-list statistics: entries of the current lists and pairs within the
+// cut-off at the last force evaluation (used for algorithmic FLOP counts).
+void device_pair_statistics(System& s, long* listed, long* within) {
+  long total = 0;
+  if (s.r0Valid) {
+    std::vector<int> cnt(s.natoms);
+    CK(cudaStreamSynchronize(s.stream));
+    CK(cudaMemcpy(cnt.data(), s.grid.dNbCount, sizeof(int) * s.natoms, cudaMemcpyDeviceToHost));
+    for (int c : cnt) total += c;
+  }
+  double w = 0.0;
+  if (s.r0Valid && s.precision == 0 && s.pairs_exist[s.layer - 1]) {
+    const double L = *s.Lbox;
+    const bool useInRc = s.useInRc[s.layer - 1] != 0;
+    device_pack(s);
+    device_pair_forces_mixed(s, false, useInRc, (useInRc ? s.InRcSq : s.RcSq) / (L * L), 2);
+    CK(cudaMemcpyAsync(&w, s.dResult + 4, sizeof(double), cudaMemcpyDeviceToHost, s.stream));
+    CK(cudaStreamSynchronize(s.stream));
+  } else {
+    CK(cudaMemcpy(&w, s.dResult + 4, sizeof(double), cudaMemcpyDeviceToHost));
+  }
+  if (listed) *listed = total / 2;
+  if (within) *within = (long)(w + 0.5);
+}
+
+}  // namespace emdee

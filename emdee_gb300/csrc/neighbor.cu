@@ -1,0 +1,713 @@
+// neighbor.cu -- skin-displacement check, cell binning into tiles and the
+// Verlet neighbor-list build (src/neighbor_lists.f90).
+//
+// The pair set is the reference's: every pair (i, j) whose minimum-image
+// distance, computed from scaled FP64 coordinates exactly as in
+// src/neighbor_lists.f90:247-250 (Rs = R/L, d = Rs_i - Rs_j, d -= anint(d),
+// r2 = dx^2 + dy^2 + dz^2), is below (rc+skin)^2/L^2, that is not excluded
+// (EmDee_ignore_pair), not in the same rigid body and whose types interact.
+// An FP32 distance in a tile-local frame decides every candidate that is
+// clearly inside or outside; candidates within a relative 4e-5 of the
+// threshold are decided by the FP64 test.  This file is compiled with
+// -fmad=false so the FP64 test rounds like the reference.
+//
+// Unlike the reference's half lists, the lists are full (each pair appears in
+// the lists of both atoms), so the force kernel owns every atom's force and
+// needs no atomics.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "system.hpp"
+#include "tile.cuh"
+
+namespace emdee {
+
+static const int NDIV = 2;   // src/EmDeeData.f90:33
+static const double BAND = 4e-5;
+
+// ---------------------------------------------------------------------------------
+// skin check: maximum_approach_sq (src/neighbor_lists.f90:41-59)
+//
+// The reference scans atoms in order, refreshing "next" only when a new
+// maximum appears.  Its result is max + 2 sqrt(max*next) + next, where
+// next = the largest value before the first occurrence of the maximum (or the
+// maximum itself when that occurrence is atom 1).  (m, p) pairs over
+// contiguous index ranges combine associatively:
+//   (mA,pA) . (mB,pB) = mB > mA ? (mB, max(mA, pB)) : (mA, pA)
+// ---------------------------------------------------------------------------------
+
+// Values are squared displacements (>= 0), so their IEEE-754 bit patterns order
+// like the values: the combine runs on 64-bit integers (-1 = none) instead of
+// the slow FP64 pipe.
+struct MaxPrev {
+  long long m, p;   // bit patterns; p < 0: no element precedes the first maximum
+};
+
+__device__ __forceinline__ MaxPrev mp_combine(MaxPrev a, MaxPrev b) {
+  if (b.m > a.m) return MaxPrev{b.m, a.m > b.p ? a.m : b.p};
+  return a;
+}
+
+static const int SKIN_THREADS = 256, SKIN_CHUNKS = 8;   // each warp: 8 x 32 consecutive atoms
+
+__device__ __forceinline__ MaxPrev warp_ordered_combine(MaxPrev acc) {
+  // after the loop lane 0 holds the combination of lanes 0..31 in lane order
+  const int lane = threadIdx.x & 31;
+  for (int o = 1; o < 32; o <<= 1) {
+    MaxPrev other{(long long)__shfl_down_sync(0xffffffffu, (unsigned long long)acc.m, o),
+                  (long long)__shfl_down_sync(0xffffffffu, (unsigned long long)acc.p, o)};
+    if ((lane & (2 * o - 1)) == 0) acc = mp_combine(acc, other);
+  }
+  return acc;
+}
+
+__global__ void __launch_bounds__(SKIN_THREADS) k_skin(const double* __restrict__ R, const double* __restrict__ R0,
+                                                       int N, double skinSq, longlong2* partial, unsigned int* ticket,
+                                                       double* result) {
+  __shared__ MaxPrev wsum[SKIN_THREADS / 32];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int base = (blockIdx.x * (SKIN_THREADS / 32) + warp) * 32 * SKIN_CHUNKS;
+  MaxPrev run{-1, -1};
+  for (int c = 0; c < SKIN_CHUNKS; c++) {
+    const int i = base + c * 32 + lane;
+    MaxPrev v{-1, -1};
+    if (i < N) {
+      double d0 = R[3 * i] - R0[3 * i], d1 = R[3 * i + 1] - R0[3 * i + 1], d2 = R[3 * i + 2] - R0[3 * i + 2];
+      v.m = __double_as_longlong(d0 * d0 + d1 * d1 + d2 * d2);
+    }
+    v = warp_ordered_combine(v);
+    run = mp_combine(run, v);   // meaningful in lane 0
+  }
+  if (lane == 0) wsum[warp] = run;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    MaxPrev b = wsum[0];
+    for (int w = 1; w < SKIN_THREADS / 32; w++) b = mp_combine(b, wsum[w]);
+    partial[blockIdx.x] = make_longlong2(b.m, b.p);
+    __threadfence();
+    last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  // last block: each warp combines a contiguous range of block partials in
+  // order, then warp results are combined in order
+  const int nb = gridDim.x, per = (nb + SKIN_THREADS - 1) / SKIN_THREADS;
+  MaxPrev acc{-1, -1};
+  for (int k = 0; k < per; k++) {
+    int b = threadIdx.x * per + k;
+    if (b < nb) {
+      longlong2 v = __ldcg(&partial[b]);
+      acc = mp_combine(acc, MaxPrev{v.x, v.y});
+    }
+  }
+  acc = warp_ordered_combine(acc);
+  if (lane == 0) wsum[warp] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    MaxPrev b = wsum[0];
+    for (int w = 1; w < SKIN_THREADS / 32; w++) b = mp_combine(b, wsum[w]);
+    double maximum = __longlong_as_double(b.m), next = __longlong_as_double(b.p < 0 ? b.m : b.p);
+    double value = maximum + 2 * sqrt(maximum * next) + next;
+    result[8] = value;
+    result[9] = value > skinSq ? 1.0 : 0.0;
+    *ticket = 0;
+  }
+}
+
+static void ensure_partials(System& s, int n) {
+  if (s.partialCap < n) {
+    CK(cudaFree(s.dPartials));
+    s.partialCap = std::max(n, 1024);
+    CK(cudaMalloc(&s.dPartials, sizeof(double) * 5 * s.partialCap));
+  }
+}
+
+bool device_skin_check(System& s) {
+  int N = s.natoms;
+  int blocks = (N + SKIN_THREADS * SKIN_CHUNKS - 1) / (SKIN_THREADS * SKIN_CHUNKS);
+  ensure_partials(s, blocks);
+  prof_begin(s, PK_SKIN);
+  k_skin<<<blocks, SKIN_THREADS, 0, s.stream>>>(s.dR, s.dR0, N, s.skinSq, (longlong2*)s.dPartials, s.dTicket,
+                                                 s.dResult);
+  CK(cudaGetLastError());
+  prof_end(s, PK_SKIN);
+  CK(cudaMemcpyAsync(s.hResult + 8, s.dResult + 8, 2 * sizeof(double), cudaMemcpyDeviceToHost, s.stream));
+  CK(cudaStreamSynchronize(s.stream));
+  return s.hResult[9] != 0.0;
+}
+
+// ---------------------------------------------------------------------------------
+// binning (src/neighbor_lists.f90:122-128) and tile sort
+// ---------------------------------------------------------------------------------
+
+__global__ void k_assign(const double* __restrict__ R, int N, double L, TileGeom g, int4* atomK, int* count) {
+  int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= N) return;
+  int c[3], K[3];
+  for (int d = 0; d < 3; d++) {
+    double rs = R[3 * a + d] / L, fl = floor(rs);
+    int ci = (int)(g.M * (rs - fl));
+    ci = ci < 0 ? 0 : (ci >= g.M ? g.M - 1 : ci);   // M*(x - floor x) may round up to M
+    c[d] = ci;
+    K[d] = (int)fl * g.M + ci;
+  }
+  int rank = cell_rank(g, c[0], c[1], c[2]);
+  atomK[a] = make_int4(K[0], K[1], K[2], rank);
+  atomicAdd(&count[rank], 1);
+}
+
+// three-phase device-wide exclusive scan (counts -> starts), starts[n] = total
+static const int SCAN_THREADS = 256, SCAN_ITEMS = 8, SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+__global__ void k_scan_local(const int* in, int* out, int n, int* blockSums) {
+  __shared__ int buf[SCAN_TILE];
+  __shared__ int ws[33];
+  int base = blockIdx.x * SCAN_TILE;
+  for (int k = threadIdx.x; k < SCAN_TILE; k += SCAN_THREADS) buf[k] = base + k < n ? in[base + k] : 0;
+  __syncthreads();
+  int total = block_exclusive_scan<SCAN_ITEMS>(buf, SCAN_TILE, ws);
+  for (int k = threadIdx.x; k < SCAN_TILE; k += SCAN_THREADS)
+    if (base + k < n) out[base + k] = buf[k];
+  if (threadIdx.x == 0) blockSums[blockIdx.x] = total;
+}
+
+__global__ void k_scan_sums(int* blockSums, int nb, int* out, int n) {
+  __shared__ int ws[33];
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < nb; base += SCAN_TILE) {
+    __shared__ int buf[SCAN_TILE];
+    for (int k = threadIdx.x; k < SCAN_TILE; k += SCAN_THREADS) buf[k] = base + k < nb ? blockSums[base + k] : 0;
+    __syncthreads();
+    int total = block_exclusive_scan<SCAN_ITEMS>(buf, SCAN_TILE, ws);
+    for (int k = threadIdx.x; k < SCAN_TILE; k += SCAN_THREADS)
+      if (base + k < nb) blockSums[base + k] = buf[k] + carry;
+    __syncthreads();
+    if (threadIdx.x == 0) carry += total;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[n] = carry;
+}
+
+__global__ void k_scan_add(int* out, int n, const int* blockSums) {
+  int base = blockIdx.x * SCAN_TILE, add = blockSums[blockIdx.x];
+  for (int k = threadIdx.x; k < SCAN_TILE; k += SCAN_THREADS)
+    if (base + k < n) out[base + k] += add;
+}
+
+static void device_scan(System& s, const int* in, int* out, int n) {
+  int nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+  k_scan_local<<<nb, SCAN_THREADS, 0, s.stream>>>(in, out, n, s.grid.dScanTmp);
+  k_scan_sums<<<1, SCAN_THREADS, 0, s.stream>>>(s.grid.dScanTmp, nb, out, n);
+  k_scan_add<<<nb, SCAN_THREADS, 0, s.stream>>>(out, n, s.grid.dScanTmp);
+  CK(cudaGetLastError());
+}
+
+__global__ void k_scatter(const int4* atomK, int N, const int* start, int* cursor, int* orig) {
+  int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= N) return;
+  int rank = atomK[a].w;
+  orig[start[rank] + atomicAdd(&cursor[rank], 1)] = a;
+}
+
+// deterministic order inside a cell: ascending atom index
+__global__ void k_sort_cells(const int* start, int nRanks, int* orig) {
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nRanks) return;
+  int b = start[r], e = start[r + 1];
+  for (int i = b + 1; i < e; i++) {
+    int v = orig[i], j = i - 1;
+    while (j >= b && orig[j] > v) {
+      orig[j + 1] = orig[j];
+      j--;
+    }
+    orig[j + 1] = v;
+  }
+}
+
+__global__ void k_fill_slots(const int* orig, int N, const int4* atomK, const int* type, int4* K, uint8_t* type8) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= N) return;
+  int a = orig[s];
+  K[s] = atomK[a];
+  type8[s] = (uint8_t)(type[a] - 1);
+}
+
+__global__ void k_halo_table(TileGeom g, int2* tab) {
+  const int t = blockIdx.x;
+  for (int h = threadIdx.x; h < g.haloCells; h += blockDim.x) tab[(size_t)t * g.haloCells + h] = halo_entry(g, t, h);
+}
+
+// per tile: number of atoms and of halo atoms; global maxima in maxOut[0..1]
+__global__ void k_tile_info(const int* start, TileGeom g, int* info, int* maxOut) {
+  __shared__ int sum;
+  int t = blockIdx.x;
+  if (threadIdx.x == 0) sum = 0;
+  __syncthreads();
+  int local = 0, hx, hy, hz;
+  for (int h = threadIdx.x; h < g.haloCells; h += blockDim.x) {
+    int r = halo_rank(g, t, h, hx, hy, hz);
+    local += start[r + 1] - start[r];
+  }
+  atomicAdd(&sum, local);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int cells = g.TB * g.TB * g.TB;
+    int n = start[(t + 1) * cells] - start[t * cells];
+    info[2 * t] = n;
+    info[2 * t + 1] = sum;
+    atomicMax(&maxOut[0], n);
+    atomicMax(&maxOut[1], sum);
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// per-step packing
+// ---------------------------------------------------------------------------------
+
+// cell-local position of each slot in units of the cell edge: u = M R/L - K
+__global__ void k_pack_mixed(const double* __restrict__ R, const double* __restrict__ charge, const int* orig,
+                             const int4* K, int N, double scale, float4* pos4) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= N) return;
+  int a = orig[s];
+  int4 k = K[s];
+  float ux = (float)(R[3 * a] * scale - (double)k.x);
+  float uy = (float)(R[3 * a + 1] * scale - (double)k.y);
+  float uz = (float)(R[3 * a + 2] * scale - (double)k.z);
+  double q = charge[a];
+  pos4[s] = make_float4(ux, uy, uz, fabs(q) > 2.220446049250313e-16 ? (float)q : 0.0f);
+}
+
+// scaled FP64 coordinates Rs = R/L (src/EmDeeCode.f90:1228) in slot order
+__global__ void k_pack_fp64(const double* __restrict__ R, const int* orig, int N, double L, double* Rs) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= N) return;
+  int a = orig[s];
+  Rs[3 * s] = R[3 * a] / L;
+  Rs[3 * s + 1] = R[3 * a + 1] / L;
+  Rs[3 * s + 2] = R[3 * a + 2] / L;
+}
+
+void device_pack(System& s) {
+  Grid& g = s.grid;
+  int N = s.natoms, th = 256, bl = (N + th - 1) / th;
+  prof_begin(s, PK_PACK);
+  if (s.precision == 1) {
+    k_pack_fp64<<<bl, th, 0, s.stream>>>(s.dR, g.dOrig, N, *s.Lbox, g.dRs64);
+  } else {
+    k_pack_mixed<<<bl, th, 0, s.stream>>>(s.dR, s.dCharge, g.dOrig, g.dK, N, (double)g.M / *s.Lbox, g.dPos4);
+  }
+  CK(cudaGetLastError());
+  prof_end(s, PK_PACK);
+}
+
+// ---------------------------------------------------------------------------------
+// list build
+// ---------------------------------------------------------------------------------
+
+
+struct BuildArgs {
+  TileGeom g;
+  const int2* tab;
+  const float4* pos4;
+  const int* start;
+  const int* orig;
+  const int4* K;
+  const uint8_t* type8;
+  const int* body;
+  int hasBodies;
+  const uint8_t* interact;
+  int ntypes;
+  const int* exFirst;
+  const int* exCount;
+  const int* exItem;
+  int hasEx;
+  const double* R;
+  double L;
+  float lo2, hi2, loIn2, hiIn2;   // FP32 band limits, cell units^2
+  double thr, thrIn;              // FP64 thresholds, scaled units^2
+  int layered;                    // inner threshold below the outer one
+  int minimg;                     // M == 5: a stencil cell may hold a non-minimum image
+  float Mf;
+  int haloCap;
+  uint16_t* nb;
+  int* nbCount;
+  int* nbInner;
+  uint16_t* selfIdx;
+  int cap, tileStride;
+  int* maxCount;
+};
+
+// FP64 minimum-image distance test of src/neighbor_lists.f90:247-250
+__device__ __noinline__ bool exact_inside(const double* R, double L, int a, int b, double thr) {
+  double d[3];
+  for (int k = 0; k < 3; k++) {
+    double x = R[3 * a + k] / L - R[3 * b + k] / L;
+    d[k] = x - round(x);
+  }
+  double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+  return r2 < thr;
+}
+
+__device__ __forceinline__ bool excluded(const BuildArgs& A, int a, int b) {
+  int f = A.exFirst[a], n = A.exCount[a];
+  for (int k = 0; k < n; k++) {
+    int v = A.exItem[f + k] - 1;
+    if (v == b) return true;
+    if (v > b) break;
+  }
+  return false;
+}
+
+static const int BUILD_THREADS = 128;
+
+// List layout: for tile t, chunk c (8 entries) and tile-local atom li, the
+// entries 8c..8c+7 of atom li are 16 contiguous bytes at
+//   nb + ((t * capC + c) * tileStride + li) * 8
+// so a warp reads one chunk of 32 consecutive atoms with one 512-byte access.
+// Unused entries of the last chunk hold the sentinel halo index haloCap.
+__device__ __forceinline__ size_t nb_index(int t, int capC, int tileStride, int li, int n) {
+  return (((size_t)t * capC + (n >> 3)) * tileStride + li) * 8 + (n & 7);
+}
+
+__global__ void __launch_bounds__(BUILD_THREADS) k_build(BuildArgs A) {
+  extern __shared__ __align__(16) unsigned char sraw[];
+  __shared__ int ws[33];
+  const TileGeom g = A.g;
+  const int t = blockIdx.x, cells = g.TB * g.TB * g.TB;
+  float4* hpos = (float4*)sraw;
+  int* hslot = (int*)(hpos + A.haloCap + 1);
+  int* off = hslot + A.haloCap + 1;
+  int* cst = off + g.haloCells + 1;
+  int* hxyz = cst + g.haloCells;
+  const bool single = A.ntypes == 1;
+  uint8_t* sinter = (uint8_t*)(hxyz + g.haloCells);
+  uint8_t* htype = sinter + A.ntypes * A.ntypes;
+  for (int k = threadIdx.x; k < A.ntypes * A.ntypes; k += blockDim.x) sinter[k] = A.interact[k];
+  halo_layout(g, t, A.tab, A.start, off, cst, hxyz, ws);
+  stage_frame(g, off, cst, hxyz, A.pos4, hpos, hslot, single ? (uint8_t*)nullptr : htype, A.type8);
+  __syncthreads();
+  const bool none = single && !sinter[0];   // the only type pair does not interact: empty lists
+  const bool filterByAtom = A.hasBodies || A.hasEx;
+  const int tb = A.start[t * cells], te = A.start[(t + 1) * cells];
+  const int HW = g.HW, capC = A.cap >> 3, chunkStride = A.tileStride * 8;
+  for (int li = threadIdx.x; li < te - tb; li += blockDim.x) {
+    const int si = tb + li;
+    const int rank = A.K[si].w, lr = rank - t * cells;
+    const int hcx = lr % g.TB + 2, hcy = (lr / g.TB) % g.TB + 2, hcz = lr / (g.TB * g.TB) + 2;
+    const int myq = off[hcx + HW * (hcy + HW * hcz)] + (si - A.start[rank]);
+    A.selfIdx[si] = (uint16_t)myq;
+    const float4 pi = hpos[myq];
+    const int ai = A.orig[si], ti = single ? 0 : A.type8[si];
+    const int bi = A.hasBodies ? A.body[ai] : -1;
+    const bool hasEx = A.hasEx && A.exCount[ai] > 0;
+    uint16_t* myList = A.nb + ((size_t)t * capC * A.tileStride + li) * 8;
+    int n = 0, nIn = 0;
+    for (int pass = 0; pass <= A.layered && !none; pass++) {
+      // the 5 cells of a stencil row (dx = -2..2) are consecutive in the halo
+      for (int row = 0; row < 25; row++) {
+        const int h0 = (hcx - 2) + HW * ((hcy + row % 5 - 2) + HW * (hcz + row / 5 - 2));
+        const int q1 = off[h0 + 5];
+        for (int q = off[h0]; q < q1; q++) {
+          const float4 pj = hpos[q];
+          float ex = pi.x - pj.x, ey = pi.y - pj.y, ez = pi.z - pj.z;
+          if (A.minimg) {
+            ex -= A.Mf * rintf(ex / A.Mf);
+            ey -= A.Mf * rintf(ey / A.Mf);
+            ez -= A.Mf * rintf(ez / A.Mf);
+          }
+          const float r2 = ex * ex + ey * ey + ez * ez;
+          if (r2 >= A.hi2 || q == myq) continue;
+          if (!(r2 < A.lo2 || exact_inside(A.R, A.L, ai, A.orig[hslot[q]], A.thr))) continue;
+          if (!single && !sinter[ti * A.ntypes + htype[q]]) continue;
+          if (filterByAtom) {
+            const int aj = A.orig[hslot[q]];
+            if (A.hasBodies && A.body[aj] == bi) continue;
+            if (hasEx && excluded(A, ai, aj)) continue;
+          }
+          if (A.layered) {
+            bool inner = r2 < A.loIn2 || (r2 < A.hiIn2 && exact_inside(A.R, A.L, ai, A.orig[hslot[q]], A.thrIn));
+            if (inner == (pass == 1)) continue;
+          }
+          if (n < A.cap) myList[(n >> 3) * chunkStride + (n & 7)] = (uint16_t)q;
+          n++;
+        }
+      }
+      if (pass == 0) nIn = n;
+    }
+    for (int k = n; k < A.cap && (k & 7); k++) myList[(k >> 3) * chunkStride + (k & 7)] = (uint16_t)A.haloCap;
+    A.nbCount[si] = n;
+    A.nbInner[si] = nIn;
+    atomicMax(A.maxCount, n);
+  }
+}
+
+template <typename T>
+static void grow(T*& p, size_t& have, size_t need) {
+  if (have >= need) return;
+  CK(cudaFree(p));
+  CK(cudaMalloc(&p, sizeof(T) * need));
+  have = need;
+}
+
+struct GridCaps {
+  size_t ranks = 0, atoms = 0, tiles = 0, nb = 0, scan = 0;
+};
+static GridCaps& caps_of(System& s) {
+  static std::vector<std::pair<System*, GridCaps>> all;
+  for (auto& p : all)
+    if (p.first == &s) return p.second;
+  all.push_back({&s, GridCaps()});
+  return all.back().second;
+}
+
+static size_t build_smem(const Grid& g, int ntypes) {
+  return (size_t)(g.maxHalo + 1) * (sizeof(float4) + sizeof(int) + 1) + 3 * sizeof(int) * (g.haloCells + 1) +
+         (size_t)ntypes * ntypes + 16;
+}
+
+static int choose_tile(int M, double perCell) {
+  if (const char* e = getenv("EMDEE_TILE")) {
+    int tb = atoi(e);
+    if (tb >= 1 && tb <= 6) return std::min(tb, M);
+  }
+  int tb = perCell <= 4.0 ? 4 : perCell <= 9.0 ? 3 : perCell <= 24.0 ? 2 : 1;
+  return std::min(tb, M);
+}
+
+// src/neighbor_lists.f90:175-195 (build part) and 199-300
+void device_build_lists(System& s) {
+  Grid& g = s.grid;
+  GridCaps& c = caps_of(s);
+  const int N = s.natoms;
+  prof_begin(s, PK_BUILD);
+  const double L = *s.Lbox;
+  int M = (int)std::floor(NDIV * L / s.xRc);
+  M = std::max(M, 2 * NDIV + 1);
+  double perCell = (double)N / ((double)M * M * M);
+  int TB = choose_tile(M, perCell);
+  size_t smemLimit = 200 * 1024;
+  for (;;) {
+    TileGeom geo = make_geom(M, TB);
+    g.M = M;
+    g.TB = TB;
+    g.nT = geo.nT;
+    g.nTiles = geo.nT * geo.nT * geo.nT;
+    g.nRanks = g.nTiles * TB * TB * TB;
+    g.haloCells = geo.haloCells;
+    grow(g.dCount, c.ranks, (size_t)g.nRanks + 1);
+    // dStart / dCursor share the rank capacity
+    if (!g.dStart || c.scan < (size_t)g.nRanks + 1) {
+      CK(cudaFree(g.dStart));
+      CK(cudaFree(g.dCursor));
+      CK(cudaFree(g.dScanTmp));
+      CK(cudaMalloc(&g.dStart, sizeof(int) * (g.nRanks + 1)));
+      CK(cudaMalloc(&g.dCursor, sizeof(int) * (g.nRanks + 1)));
+      CK(cudaMalloc(&g.dScanTmp, sizeof(int) * ((g.nRanks + SCAN_TILE) / SCAN_TILE + 1)));
+      c.scan = (size_t)g.nRanks + 1;
+    }
+    if (c.atoms < (size_t)N) {
+      CK(cudaFree(g.dOrig)); CK(cudaFree(g.dK)); CK(cudaFree(g.dAtomK)); CK(cudaFree(g.dPos4));
+      CK(cudaFree(g.dType8)); CK(cudaFree(g.dRs64)); CK(cudaFree(g.dNbCount)); CK(cudaFree(g.dNbInner));
+      CK(cudaFree(g.dSelf));
+      CK(cudaMalloc(&g.dOrig, sizeof(int) * N));
+      CK(cudaMalloc(&g.dK, sizeof(int4) * N));
+      CK(cudaMalloc(&g.dAtomK, sizeof(int4) * N));
+      CK(cudaMalloc(&g.dPos4, sizeof(float4) * N));
+      CK(cudaMalloc(&g.dType8, N));
+      CK(cudaMalloc(&g.dRs64, sizeof(double) * 3 * N));
+      CK(cudaMalloc(&g.dNbCount, sizeof(int) * N));
+      CK(cudaMalloc(&g.dNbInner, sizeof(int) * N));
+      CK(cudaMalloc(&g.dSelf, sizeof(uint16_t) * N));
+      c.atoms = N;
+    }
+    if (c.tiles < (size_t)g.nTiles) {
+      CK(cudaFree(g.dTileInfo));
+      CK(cudaMalloc(&g.dTileInfo, sizeof(int) * (2 * g.nTiles + 4)));
+      c.tiles = g.nTiles;
+    }
+    int th = 256, bl = (N + th - 1) / th;
+    CK(cudaMemsetAsync(g.dCount, 0, sizeof(int) * (g.nRanks + 1), s.stream));
+    CK(cudaMemsetAsync(g.dCursor, 0, sizeof(int) * (g.nRanks + 1), s.stream));
+    s.prof.total += 8;   // assign, 3 scan phases, scatter, sort, fill, tile info
+    k_assign<<<bl, th, 0, s.stream>>>(s.dR, N, L, geo, g.dAtomK, g.dCount);
+    CK(cudaGetLastError());
+    device_scan(s, g.dCount, g.dStart, g.nRanks);
+    k_scatter<<<bl, th, 0, s.stream>>>(g.dAtomK, N, g.dStart, g.dCursor, g.dOrig);
+    k_sort_cells<<<(g.nRanks + 255) / 256, 256, 0, s.stream>>>(g.dStart, g.nRanks, g.dOrig);
+    k_fill_slots<<<bl, th, 0, s.stream>>>(g.dOrig, N, g.dAtomK, s.dType, g.dK, g.dType8);
+    int* dMax = g.dTileInfo + 2 * g.nTiles;
+    CK(cudaMemsetAsync(dMax, 0, sizeof(int) * 4, s.stream));
+    k_tile_info<<<g.nTiles, 128, 0, s.stream>>>(g.dStart, geo, g.dTileInfo, dMax);
+    CK(cudaGetLastError());
+    int hmax[2];
+    CK(cudaMemcpyAsync(hmax, dMax, sizeof(int) * 2, cudaMemcpyDeviceToHost, s.stream));
+    CK(cudaStreamSynchronize(s.stream));
+    {
+      size_t need = (size_t)g.nTiles * g.haloCells;
+      if (g.haloTabCap < need) {
+        CK(cudaFree(g.dHaloTab));
+        CK(cudaMalloc(&g.dHaloTab, sizeof(int2) * need));
+        g.haloTabCap = need;
+      }
+      k_halo_table<<<g.nTiles, 128, 0, s.stream>>>(geo, g.dHaloTab);
+      CK(cudaGetLastError());
+      s.prof.total++;
+    }
+    g.tileStride = std::max(32, (hmax[0] + 31) / 32 * 32);
+    g.maxHalo = hmax[1];
+    size_t smem = build_smem(g, s.ntypes);
+    size_t smem64 = (size_t)(g.maxHalo + 1) * (4 * sizeof(double) + 1) + 2 * sizeof(int) * (g.haloCells + 1) + 64;
+    if ((g.maxHalo > 65534 || smem > smemLimit || (s.precision == 1 && smem64 > smemLimit)) && TB > 1) {
+      TB--;
+      continue;
+    }
+    if (g.maxHalo > 65534 || smem > smemLimit) fatal("neighbor list build", "too many atoms around a cell");
+    break;
+  }
+  TileGeom geo = make_geom(g.M, g.TB);
+  // neighbor capacity: expected full-list count with margin, grown on overflow
+  if (g.cap == 0) {
+    double rho = N / (L * L * L);
+    double expected = rho * 4.18879020478639 * s.xRcSq * s.xRc;
+    g.cap = (int)std::min(65528.0, expected * 1.35 + 32);
+  }
+  g.cap = (g.cap + 7) / 8 * 8;
+  const double invL2 = 1.0 / (L * L);
+  BuildArgs A;
+  A.g = geo;
+  A.tab = g.dHaloTab;
+  A.pos4 = g.dPos4;
+  A.start = g.dStart;
+  A.orig = g.dOrig;
+  A.K = g.dK;
+  A.type8 = g.dType8;
+  A.body = s.dBody;
+  A.hasBodies = s.nbodies > 0;
+  A.interact = s.models.interact;
+  A.ntypes = s.ntypes;
+  A.exFirst = s.dExFirst;
+  A.exCount = s.dExCount;
+  A.exItem = s.dExItem;
+  A.hasEx = s.hasExclusions;
+  A.R = s.dR;
+  A.L = L;
+  A.thr = s.xRcSq * invL2;    // src/neighbor_lists.f90:213-214
+  A.thrIn = s.xInRcSq * invL2;
+  double M2 = (double)g.M * g.M;
+  A.lo2 = (float)(A.thr * M2 * (1.0 - BAND));
+  A.hi2 = (float)(A.thr * M2 * (1.0 + BAND));
+  A.loIn2 = (float)(A.thrIn * M2 * (1.0 - BAND));
+  A.hiIn2 = (float)(A.thrIn * M2 * (1.0 + BAND));
+  A.layered = s.xInRcSq < s.xRcSq ? 1 : 0;
+  A.minimg = g.M == 5 ? 1 : 0;
+  A.Mf = (float)g.M;
+  A.haloCap = g.maxHalo;
+  A.nbCount = g.dNbCount;
+  A.nbInner = g.dNbInner;
+  A.selfIdx = g.dSelf;
+  A.tileStride = g.tileStride;
+  A.maxCount = g.dTileInfo + 2 * g.nTiles + 2;
+  // positions for the FP32 prefilter
+  {
+    int th = 256, bl = (N + th - 1) / th;
+    k_pack_mixed<<<bl, th, 0, s.stream>>>(s.dR, s.dCharge, g.dOrig, g.dK, N, (double)g.M / L, g.dPos4);
+    CK(cudaGetLastError());
+    s.prof.total++;
+  }
+  size_t smem = build_smem(g, s.ntypes);
+  CK(cudaFuncSetAttribute(k_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  for (int attempt = 0; attempt < 3; attempt++) {
+    size_t need = (size_t)g.nTiles * g.cap * g.tileStride;
+    grow(g.dNb, c.nb, need);
+    A.nb = g.dNb;
+    A.cap = g.cap;
+    CK(cudaMemsetAsync(A.maxCount, 0, sizeof(int), s.stream));
+    k_build<<<g.nTiles, BUILD_THREADS, smem, s.stream>>>(A);
+    s.prof.total++;
+    CK(cudaGetLastError());
+    int mc = 0;
+    CK(cudaMemcpyAsync(&mc, A.maxCount, sizeof(int), cudaMemcpyDeviceToHost, s.stream));
+    CK(cudaStreamSynchronize(s.stream));
+    if (mc <= g.cap) break;
+    if (mc > 65528) fatal("neighbor list build", "more than 65528 neighbors for one atom");
+    g.cap = std::min(65528, (mc + mc / 8 + 16 + 7) / 8 * 8);
+  }
+  CK(cudaMemcpyAsync(s.dR0, s.dR, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, s.stream));
+  prof_end(s, PK_BUILD);
+  s.r0Valid = true;
+  s.builtL = L;
+}
+
+// ---------------------------------------------------------------------------------
+// pair-set dump (test support): every full-list entry as (orig_i, orig_j)
+// ---------------------------------------------------------------------------------
+
+__global__ void k_dump_pairs(TileGeom g, const int2* tab, const int* start, const int* orig, const uint16_t* nb,
+                             const int* nbCount, int cap, int tileStride, const long long* outStart, int2* out) {
+  extern __shared__ int hslot[];
+  __shared__ int ws[33];
+  __shared__ int off[1001], cst[1000];
+  const int t = blockIdx.x, cells = g.TB * g.TB * g.TB;
+  halo_layout(g, t, tab, start, off, cst, (int*)nullptr, ws);
+  for (int h = threadIdx.x; h < g.haloCells; h += blockDim.x)
+    for (int k = off[h]; k < off[h + 1]; k++) hslot[k] = cst[h] + (k - off[h]);
+  __syncthreads();
+  const int tb = start[t * cells], te = start[(t + 1) * cells];
+  for (int li = threadIdx.x; li < te - tb; li += blockDim.x) {
+    int si = tb + li, ai = orig[si];
+    long long o = outStart[si];
+    for (int k = 0; k < nbCount[si]; k++) {
+      int q = nb[nb_index(t, cap >> 3, tileStride, li, k)];
+      out[o + k] = make_int2(ai + 1, orig[hslot[q]] + 1);
+    }
+  }
+}
+
+long device_neighbor_pairs(System& s, int* pairs, long capacity) {
+  Grid& g = s.grid;
+  int N = s.natoms;
+  if (!s.r0Valid) return 0;
+  std::vector<int> cnt(N), orig(N);
+  CK(cudaStreamSynchronize(s.stream));
+  CK(cudaMemcpy(cnt.data(), g.dNbCount, sizeof(int) * N, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(orig.data(), g.dOrig, sizeof(int) * N, cudaMemcpyDeviceToHost));
+  std::vector<long long> st(N + 1, 0);
+  for (int i = 0; i < N; i++) st[i + 1] = st[i] + cnt[i];
+  long long total = st[N];
+  long npairs = (long)(total / 2);
+  if (npairs > capacity) return -npairs;
+  long long* dSt;
+  int2* dOut;
+  CK(cudaMalloc(&dSt, sizeof(long long) * (N + 1)));
+  CK(cudaMalloc(&dOut, sizeof(int2) * (total + 1)));
+  CK(cudaMemcpy(dSt, st.data(), sizeof(long long) * (N + 1), cudaMemcpyHostToDevice));
+  TileGeom geo = make_geom(g.M, g.TB);
+  k_dump_pairs<<<g.nTiles, 128, sizeof(int) * g.maxHalo, s.stream>>>(geo, g.dHaloTab, g.dStart, g.dOrig, g.dNb,
+                                                                      g.dNbCount, g.cap, g.tileStride, dSt, dOut);
+  CK(cudaGetLastError());
+  std::vector<int2> h(total);
+  CK(cudaStreamSynchronize(s.stream));
+  CK(cudaMemcpy(h.data(), dOut, sizeof(int2) * total, cudaMemcpyDeviceToHost));
+  CK(cudaFree(dSt));
+  CK(cudaFree(dOut));
+  std::vector<std::pair<int, int>> v;
+  v.reserve(npairs);
+  for (auto& e : h)
+    if (e.x < e.y) v.push_back({e.x, e.y});
+  std::sort(v.begin(), v.end());
+  long n = (long)v.size();
+  if (n > capacity) return -n;
+  for (long k = 0; k < n; k++) {
+    pairs[2 * k] = v[k].first;
+    pairs[2 * k + 1] = v[k].second;
+  }
+  return n;
+}
+
+}  // namespace emdee

@@ -1,0 +1,220 @@
+// pair_mixed.cu -- pair forces, energies and virials with FP32 pair arithmetic
+// and FP64 energy/virial accumulation (src/compute.f90:20-100,
+// src/EmDeeData.f90:644-685).
+//
+// One thread block per tile.  The block stages its halo (tile + 2 cells on each
+// side) in shared memory as FP32 positions in a tile-local frame, in units of
+// the cell edge, so a pair distance is one subtraction per component with no
+// periodic image arithmetic (except when M = 5, where a stencil cell can be a
+// non-minimum image).  Each thread owns one atom i and walks its full neighbor
+// list (16-bit halo indices, coalesced across the warp), accumulating F_i in
+// registers: Newton's third law is not used, so no atomics touch the forces.
+// Per-thread energy and virial sums are promoted to FP64 for the block and grid
+// reductions.
+#include <algorithm>
+
+#include "reduce.cuh"
+#include "system.hpp"
+#include "tile.cuh"
+
+namespace emdee {
+
+static const int PAIR_THREADS = 256;   // upper bound; launches use one thread per tile atom
+
+struct PairArgsF {
+  TileGeom g;
+  const int2* tab;
+  const float4* pos4;
+  const uint8_t* type8;
+  const int* start;
+  const int* orig;
+  const uint16_t* self;
+  const uint16_t* nb;
+  const int* count;
+  int cap, tileStride, haloCap;
+  const PairEntry<float>* table;   // this layer: [itype][jtype] -> pair(jtype, itype)
+  const NBParams<float>* coul;
+  int ntypes;
+  float rc2;     // cutoff^2 in cell units^2
+  float invw2;   // 1/w^2, w = L/M (cell edge)
+  float invw;
+  float Mf;
+  double* F;     // forces, API order, double[N][3]
+  double* partials;
+  unsigned int* ticket;
+  double* result;
+};
+
+// VAR 0: one atom type, Lennard-Jones with modifier MOD, no Coulomb term.
+// VAR 1: any types, any pair model and modifier, Coulomb term.
+// COUNT: also count the pairs within the cut-off (statistics launches only).
+// Lists are read 8 entries (16 bytes) per lane at a time, one chunk ahead of
+// use; padding entries point at a sentinel halo slot far from every atom, so
+// the inner loop needs no bounds test (except when M = 5, where the periodic
+// wrap would bring the sentinel back).
+template <bool COMPUTE, int VAR, int MOD, bool MINIMG, bool COUNT>
+__global__ void __launch_bounds__(PAIR_THREADS) k_pair_mixed(PairArgsF A) {
+  extern __shared__ __align__(16) unsigned char sraw[];
+  __shared__ int ws[33];
+  const TileGeom g = A.g;
+  const int t = blockIdx.x, cells = g.TB * g.TB * g.TB;
+  float4* hpos = (float4*)sraw;
+  int* off = (int*)(hpos + A.haloCap + 1);
+  int* cst = off + g.haloCells + 1;
+  int* hxyz = cst + g.haloCells;
+  PairEntry<float>* tbl = (PairEntry<float>*)(hxyz + g.haloCells);
+  const int ntab = VAR == 1 ? A.ntypes * A.ntypes : 0;
+  uint8_t* htype = (uint8_t*)(tbl + ntab);
+  for (int k = threadIdx.x; k < ntab; k += blockDim.x) tbl[k] = A.table[k];
+  if (threadIdx.x == 0) {
+    hpos[A.haloCap] = make_float4(1e9f, 1e9f, 1e9f, 0.f);
+    if (VAR == 1) htype[A.haloCap] = 0;
+  }
+  halo_layout(g, t, A.tab, A.start, off, cst, hxyz, ws);
+  stage_frame(g, off, cst, hxyz, A.pos4, hpos, (int*)nullptr, VAR == 1 ? htype : (uint8_t*)nullptr, A.type8);
+  __syncthreads();
+
+  NBParams<float> m0 = A.table[0].model;
+  if (VAR == 0) m0.modifier = MOD;
+  NBParams<float> coul;
+  if (VAR == 1) coul = *A.coul;
+  const int tb = A.start[t * cells], te = A.start[(t + 1) * cells];
+  const int capC = A.cap >> 3;
+  float Ep = 0.f, Ec = 0.f, Wp = 0.f, Wc = 0.f, within = 0.f;
+  for (int li = threadIdx.x; li < te - tb; li += blockDim.x) {
+    const int si = tb + li;
+    const int qi = A.self[si];
+    const float4 pi = hpos[qi];
+    const int n = min(A.count[si], A.cap);
+    const int nch = (n + 7) >> 3;
+    const uint4* lp = reinterpret_cast<const uint4*>(A.nb) + ((size_t)t * capC * A.tileStride + li);
+    const int ti = VAR == 1 ? htype[qi] : 0;
+    float fx = 0.f, fy = 0.f, fz = 0.f;
+    uint4 cur = nch > 0 ? __ldcs(lp) : make_uint4(0u, 0u, 0u, 0u);
+    for (int c = 0; c < nch; c++) {
+      const uint4 nxt = (c + 1 < nch) ? __ldcs(lp + (size_t)(c + 1) * A.tileStride) : cur;
+      const unsigned w[4] = {cur.x, cur.y, cur.z, cur.w};
+#pragma unroll
+      for (int e = 0; e < 8; e++) {
+        if (MINIMG && c * 8 + e >= n) break;
+        const int qj = (w[e >> 1] >> ((e & 1) * 16)) & 0xFFFF;
+        const float4 pj = hpos[qj];
+        float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+        if (MINIMG) {
+          dx -= A.Mf * rintf(dx / A.Mf);
+          dy -= A.Mf * rintf(dy / A.Mf);
+          dz -= A.Mf * rintf(dz / A.Mf);
+        }
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        if (r2 < A.rc2) {
+          if (COUNT) within += 1.f;
+          const float invR2c = Ops<float>::rcp(r2);
+          const float invR2 = invR2c * A.invw2;
+          float Wsum;
+          if (VAR == 0) {
+            constexpr bool needR = MOD == SHIFTED_FORCE || MOD == SMOOTHED || MOD == SHIFTED_SMOOTHED;
+            const float invR = needR ? sqrtf(invR2) : 1.f;
+            float sr2 = m0.sigsq * invR2, sr6 = sr2 * sr2 * sr2, sr12 = sr6 * sr6;
+            float E = m0.eps4 * (sr12 - sr6), W = m0.eps24 * (sr12 + sr12 - sr6);
+            if (MOD != NONE) modifier_compute(m0, E, W, invR, invR2);
+            if (COMPUTE) Ep += E;
+            Wp += W;
+            Wsum = W;
+          } else {
+            const int tj = htype[qj];
+            const PairEntry<float>& pe = tbl[ti * A.ntypes + tj];
+            const float invR = sqrtf(invR2);
+            const bool ijch = pi.w != 0.f && pj.w != 0.f;
+            Wsum = pair_eval<float, COMPUTE>(pe, coul, ijch, pi.w, pj.w, invR, invR2, Ep, Ec, Wp, Wc);
+          }
+          const float s = Wsum * invR2c;
+          fx += s * dx;
+          fy += s * dy;
+          fz += s * dz;
+        }
+      }
+      cur = nxt;
+    }
+    if (!COUNT) {
+      double* Fa = A.F + 3 * (size_t)A.orig[si];
+      Fa[0] = f2d_exact(fx * A.invw);
+      Fa[1] = f2d_exact(fy * A.invw);
+      Fa[2] = f2d_exact(fz * A.invw);
+    }
+  }
+  // each pair is visited from both atoms: halve the sums
+  const float v[5] = {0.5f * Ep, 0.5f * Ec, 0.5f * Wp, 0.5f * Wc, 0.5f * within};
+  grid_reduce_f32<5, PAIR_THREADS>(v, A.partials, A.ticket, A.result);
+}
+
+template <bool COMPUTE, int VAR, int MOD, bool MINIMG, bool COUNT>
+static void launch(System& s, PairArgsF& A, size_t smem, int nTiles, int threads) {
+  auto kern = k_pair_mixed<COMPUTE, VAR, MOD, MINIMG, COUNT>;
+  static size_t configured = 0;
+  if (smem > configured) {
+    CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    configured = smem;
+  }
+  kern<<<nTiles, threads, smem, s.stream>>>(A);
+}
+
+template <bool COMPUTE, bool MINIMG>
+static void launch_lj(System& s, PairArgsF& A, size_t smem, int nt, int th, int mod) {
+  switch (mod) {
+    case NONE: launch<COMPUTE, 0, NONE, MINIMG, false>(s, A, smem, nt, th); break;
+    case SHIFTED: launch<COMPUTE, 0, SHIFTED, MINIMG, false>(s, A, smem, nt, th); break;
+    case SHIFTED_FORCE: launch<COMPUTE, 0, SHIFTED_FORCE, MINIMG, false>(s, A, smem, nt, th); break;
+    case SMOOTHED: launch<COMPUTE, 0, SMOOTHED, MINIMG, false>(s, A, smem, nt, th); break;
+    case SHIFTED_SMOOTHED: launch<COMPUTE, 0, SHIFTED_SMOOTHED, MINIMG, false>(s, A, smem, nt, th); break;
+    case SQUARE_SMOOTHED: launch<COMPUTE, 0, SQUARE_SMOOTHED, MINIMG, false>(s, A, smem, nt, th); break;
+    default: launch<COMPUTE, 0, SHIFTED_SQUARE_SMOOTHED, MINIMG, false>(s, A, smem, nt, th); break;
+  }
+}
+
+// variant: 0 single-type Lennard-Jones without charges, 1 general, 2 pair count only
+void device_pair_forces_mixed(System& s, bool compute, bool useInRc, double rc2scaled, int variant) {
+  Grid& g = s.grid;
+  const double L = *s.Lbox, w = L / g.M;
+  PairArgsF A;
+  A.g = make_geom(g.M, g.TB);
+  A.tab = g.dHaloTab;
+  A.pos4 = g.dPos4;
+  A.type8 = g.dType8;
+  A.start = g.dStart;
+  A.orig = g.dOrig;
+  A.self = g.dSelf;
+  A.nb = g.dNb;
+  A.count = useInRc ? g.dNbInner : g.dNbCount;
+  A.cap = g.cap;
+  A.tileStride = g.tileStride;
+  A.haloCap = g.maxHalo;
+  A.table = s.models.d32 + (size_t)(s.layer - 1) * s.ntypes * s.ntypes;
+  A.coul = s.models.coul32 + (s.layer - 1);
+  A.ntypes = s.ntypes;
+  A.rc2 = (float)(rc2scaled * (double)g.M * g.M);
+  A.invw2 = (float)(1.0 / (w * w));
+  A.invw = (float)(1.0 / w);
+  A.Mf = (float)g.M;
+  A.F = s.F();
+  A.partials = s.dPartials;
+  A.ticket = s.dTicket;
+  A.result = s.dResult;
+  size_t smem = (size_t)(g.maxHalo + 1) * sizeof(float4) + sizeof(int) * (3 * g.haloCells + 1);
+  if (variant != 0) smem += sizeof(PairEntry<float>) * s.ntypes * s.ntypes + g.maxHalo + 17;
+  const bool mi = g.M == 5;
+  const int th = std::min(PAIR_THREADS, std::max(32, g.tileStride));
+  const int nt = g.nTiles;
+  if (variant == 0) {
+    const int mod = s.P(0, 0, s.layer - 1).model.p.modifier;
+    if (compute) { if (mi) launch_lj<true, true>(s, A, smem, nt, th, mod); else launch_lj<true, false>(s, A, smem, nt, th, mod); }
+    else { if (mi) launch_lj<false, true>(s, A, smem, nt, th, mod); else launch_lj<false, false>(s, A, smem, nt, th, mod); }
+  } else if (variant == 1) {
+    if (compute) { if (mi) launch<true, 1, -1, true, false>(s, A, smem, nt, th); else launch<true, 1, -1, false, false>(s, A, smem, nt, th); }
+    else { if (mi) launch<false, 1, -1, true, false>(s, A, smem, nt, th); else launch<false, 1, -1, false, false>(s, A, smem, nt, th); }
+  } else {
+    if (mi) launch<false, 1, -1, true, true>(s, A, smem, nt, th); else launch<false, 1, -1, false, true>(s, A, smem, nt, th);
+  }
+  CK(cudaGetLastError());
+}
+
+}  // namespace emdee

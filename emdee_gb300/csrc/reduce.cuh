@@ -1,0 +1,95 @@
+// reduce.cuh -- deterministic block and grid reductions of FP64 partial sums.
+//
+// THREADS is the largest block size the kernel is launched with.  Each block reduces its per-thread values (warp shuffles, then warps in
+// order) and writes one partial per quantity; the last block to finish (ticket
+// counter) sums the partials in block order with Neumaier compensation.  The
+// result does not depend on block scheduling.
+#pragma once
+
+namespace emdee {
+
+// Variant whose inputs are already warp sums held by lane 0 of each warp.
+template <int NQ, int THREADS>
+__device__ __forceinline__ void grid_reduce_lane0(const double (&v)[NQ], double* partials, unsigned int* ticket,
+                                                  double* result) {
+  __shared__ double red[NQ][THREADS / 32];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < NQ; q++) red[q][warp] = v[q];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < NQ; q++) {
+      double x = 0.0;
+      for (int w = 0; w < nw; w++) x += red[q][w];
+      partials[(size_t)blockIdx.x * NQ + q] = x;
+    }
+    __threadfence();
+    last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  // last block: thread t sums partials t, t + blockDim, ... (Neumaier), then the
+  // per-thread sums are combined by a fixed tree; the order never depends on
+  // which block finished last.
+#pragma unroll
+  for (int q = 0; q < NQ; q++) {
+    double s = 0.0, c = 0.0;
+    for (unsigned int b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+      double x = __ldcg(&partials[(size_t)b * NQ + q]);
+      double t = s + x;
+      c += fabs(s) >= fabs(x) ? (s - t) + x : (x - t) + s;
+      s = t;
+    }
+    double x = s + c;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) red[q][warp] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < NQ) {
+    double x = 0.0;
+    for (int w = 0; w < nw; w++) x += red[threadIdx.x][w];
+    result[threadIdx.x] = x;
+  }
+  if (threadIdx.x == 0) *ticket = 0;
+}
+
+// FP64 per-thread values: warp shuffle sums, then as above.
+template <int NQ, int THREADS>
+__device__ __forceinline__ void grid_reduce(double (&v)[NQ], double* partials, unsigned int* ticket, double* result) {
+#pragma unroll
+  for (int q = 0; q < NQ; q++)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_down_sync(0xffffffffu, v[q], o);
+  grid_reduce_lane0<NQ, THREADS>(v, partials, ticket, result);
+}
+
+// Warp sum of FP32 values with an error-free two-sum at every level; lane 0
+// returns hi + lo in FP64.
+__device__ __forceinline__ double warp_sum_f32(float x) {
+  float hi = x, lo = 0.f;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    float h2 = __shfl_down_sync(0xffffffffu, hi, o), l2 = __shfl_down_sync(0xffffffffu, lo, o);
+    float s = hi + h2, bp = s - hi, err = (hi - (s - bp)) + (h2 - bp);
+    hi = s;
+    lo = lo + l2 + err;
+  }
+  return (double)hi + (double)lo;
+}
+
+// grid_reduce for per-thread FP32 partial sums: compensated warp sums in FP32,
+// FP64 from there on.
+template <int NQ, int THREADS>
+__device__ __forceinline__ void grid_reduce_f32(const float (&v)[NQ], double* partials, unsigned int* ticket,
+                                                double* result) {
+  double w[NQ];
+#pragma unroll
+  for (int q = 0; q < NQ; q++) w[q] = warp_sum_f32(v[q]);
+  grid_reduce_lane0<NQ, THREADS>(w, partials, ticket, result);
+}
+
+}  // namespace emdee

@@ -1,0 +1,206 @@
+// system.hpp -- state of one EmDee system: host-side configuration that mirrors
+// the reference's tData (src/EmDeeData.f90:66-151) and the device-resident
+// arrays of the GB300 implementation.
+//
+// Layout in HBM
+//   per atom, API (original) order:  R, P, R0 (double[N][3]), F per layer
+//       (double[nlayers][N][3]), invMass, charge (double), type, body (int)
+//   per slot, tile-sorted order:     orig (slot -> atom), K (int4 image-cell of
+//       the atom at the last build), pos4 (float4 cell-local position + charge),
+//       type8 (uint8), Rs64 (double[3], FP64 mode), neighbor counts
+//   neighbor lists: uint16 halo indices, tile-major ELL blocks
+//       nb[(tile * cap + k) * tileStride + local]
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <string>
+#include <vector>
+
+#include "../../include/emdee.h"
+#include "pairmath.cuh"
+
+namespace emdee {
+
+[[noreturn]] void fatal(const char* task, const char* msg);
+void warn(const char* msg);
+void cuda_check(cudaError_t e, const char* what);
+#define CK(call) ::emdee::cuda_check((call), #call)
+
+// ---- models -------------------------------------------------------------
+
+enum ModelClass : int { MC_PAIR = 1, MC_COUL, MC_BOND, MC_ANGLE, MC_DIHEDRAL, MC_KSPACE };
+
+// A model handle as delivered to the caller (src/modelClass.f90:51-60).
+struct Model {
+  int cls = 0, kind = 0;
+  char name[24] = {0};
+  double epsilon = 0, sigma = 0, lambda = 0, damp = 0, skinWidth = 0, accuracy = 0, k = 0, x0 = 0;
+  double skin = 0, RmSq = 0;   // cNonBondedModel fields not used by the kernels
+  int shifted = 0, shifted_force = 0, requires_kspace = 0;
+  NBParams<double> p{};        // set-up result evaluated by the kernels
+};
+
+struct PairHost {   // pairContainer (src/modelClass_pair.f90:60-68)
+  Model model;
+  int coulomb = 0;
+  double kCoul = 0;
+};
+
+Model model_new(int cls, int kind, const char* name);
+Model lj_setup(double eps, double sig);
+Model softcore_setup(double eps, double sig, double lambda);
+void modifier_setup(Model& m, double cutoff);
+void cutoff_setup(Model& m, double cutoff);
+PairHost pair_container_mix(const PairHost& a, const PairHost& b);
+
+// ---- KISS + ziggurat generator (src/math.f90:69-177) -----------------------
+
+struct Kiss {
+  bool seeding_required = true;
+  int32_t kn[128];
+  double wn[128], fn[128];
+  uint32_t x, y, z, w;
+  void setup(int32_t seed);
+  int32_t i32();
+  double normal();
+};
+
+// ---- neighbor machinery ------------------------------------------------------
+
+struct Grid {
+  int M = 0;            // cells per dimension (src/neighbor_lists.f90:185-186)
+  int TB = 0;           // tile edge in cells
+  int nT = 0;           // tiles per dimension
+  int nTiles = 0, nRanks = 0, haloCells = 0;
+  int cap = 0;          // neighbor capacity per atom
+  int tileStride = 0;   // max atoms per tile, padded to a multiple of 32
+  int maxHalo = 0;      // max halo atoms over tiles
+  size_t nbBytes = 0;
+  int *dCount = nullptr, *dStart = nullptr, *dCursor = nullptr, *dScanTmp = nullptr;
+  int* dOrig = nullptr;
+  uint16_t* dSelf = nullptr;   // halo index of each slot in its own tile
+  int4* dK = nullptr;
+  int4* dAtomK = nullptr;
+  float4* dPos4 = nullptr;
+  uint8_t* dType8 = nullptr;
+  double* dRs64 = nullptr;
+  uint16_t* dNb = nullptr;
+  int *dNbCount = nullptr, *dNbInner = nullptr;
+  int* dTileInfo = nullptr;   // per tile: atoms, halo atoms
+  int2* dHaloTab = nullptr;   // per tile and halo cell: rank, packed halo coordinates
+  size_t haloTabCap = 0;
+};
+
+struct DevModels {   // per-layer pair tables uploaded for the kernels
+  PairEntry<double>* d64 = nullptr;
+  PairEntry<float>* d32 = nullptr;
+  NBParams<double>* coul64 = nullptr;
+  NBParams<float>* coul32 = nullptr;
+  uint8_t* interact = nullptr;
+};
+
+// Per-kernel CUDA-event timing (EmDee_profile / EmDee_kernel_times).
+enum ProfKind : int { PK_SKIN = 0, PK_BUILD, PK_PACK, PK_PAIR, PK_BOOST, PK_MOVE, PK_COUNT };
+struct Prof {
+  bool on = false;
+  std::vector<cudaEvent_t> pool;
+  std::vector<int> kind;          // per pending pair of events
+  std::vector<cudaEvent_t> ev;    // start, end, start, end, ...
+  double ms[PK_COUNT] = {0};
+  long launches[PK_COUNT] = {0};
+  long total = 0;                 // kernels launched since the system was created
+};
+
+struct System {
+  // configuration (src/EmDeeData.f90:66-151)
+  int natoms = 0, ntypes = 1, nlayers = 1, layer = 1, nthreads = 1;
+  double Rc = 0, skin = 0, RcSq = 0, xRc = 0, xRcSq = 0, skinSq = 0, InRc = 0, InRcSq = 0, xInRcSq = 0;
+  double totalMass = 0, startTime = 0;
+  double* Lbox = nullptr;   // host scalar, shared by EmDee_share_phase_space
+  bool ownsLbox = true;
+  bool initialized = false;
+  int precision = 0;        // 0 mixed (FP32 pair math), 1 FP64
+  Kiss random;
+
+  std::vector<int> atomType, atomBody;
+  std::vector<double> mass, invMass, charge;
+  std::vector<char> charged;
+  int nfree = 0, nbodies = 0;
+  bool unitMass = true;   // every mass is exactly 1
+  std::vector<int> exFirst, exLast, exItem;   // sorted exclusion lists, 1-based items
+  std::vector<PairHost> pair;                 // [layer][jtype][itype]
+  std::vector<Model> coul;                    // per layer
+  Model kspace;
+  bool kspace_active = false;
+  std::vector<char> multilayer, overridable, interact, pairs_exist, useInRc, bonded, forcesUpToDate;
+  std::vector<tEnergy> layerEnergy;
+  std::vector<tVirial> layerVirial;
+  bool multilayer_coulomb = false;
+  bool hasR = false;
+
+  // device state
+  cudaStream_t stream = nullptr;
+  double *dR = nullptr, *dP = nullptr, *dR0 = nullptr, *dLayerF = nullptr;
+  bool ownsRP = true;
+  double *dInvMass = nullptr, *dCharge = nullptr;
+  int *dType = nullptr, *dBody = nullptr;
+  int *dExFirst = nullptr, *dExCount = nullptr, *dExItem = nullptr;
+  bool hasExclusions = false;
+  Grid grid;
+  DevModels models;
+  bool modelsUploaded = false;
+  bool r0Valid = false;        // R0 holds the positions of the last build
+  double builtL = 0;           // box length at the last build
+
+  // reduction scratch
+  double* dPartials = nullptr;   // per tile: Epair, Ecoul, Wpair, Wcoul, pairs within rc
+  int partialCap = 0;
+  double* dKE = nullptr;         // per block: 2KE x, y, z
+  int keCap = 0;
+  unsigned int* dTicket = nullptr;
+  // results (pinned host copy and device): [0..3] Epair, Ecoul, Wpair, Wcoul, [4] pairs within
+  // the cut-off, [8] skin value, [9] rebuild flag, [10..12] 2KE per dimension
+  double* hResult = nullptr;
+  double* dResult = nullptr;
+
+  Prof prof;
+
+  // host mirrors handed out by EmDee_memory_address
+  double *hMirrorR = nullptr, *hMirrorP = nullptr, *hMirrorF = nullptr, *hMirrorLayerF = nullptr;
+
+  double* F() const { return dLayerF + (size_t)3 * natoms * (layer - 1); }
+  PairHost& P(int itype, int jtype, int l) {   // 0-based
+    return pair[((size_t)l * ntypes + jtype) * ntypes + itype];
+  }
+  char& T2(std::vector<char>& a, int i, int j) { return a[(size_t)j * ntypes + i]; }
+};
+
+System* sys_of(const tEmDee& md);
+void prof_begin(System& s, int kind);
+void prof_end(System& s, int kind);
+
+// ---- device entry points (neighbor.cu, pair_*.cu, motion.cu) ---------------------
+
+// Skin-displacement check of src/neighbor_lists.f90:41-59,184; returns true when
+// the lists must be rebuilt.  Synchronizes the stream.
+bool device_skin_check(System& s);
+// Cell binning, tile sort and neighbor-list build (src/neighbor_lists.f90:63-300).
+void device_build_lists(System& s);
+// Per-step position packing for the force kernels.
+void device_pack(System& s);
+// Pair forces, energies and virials of the current layer into s.F();
+// leaves Epair, Ecoul, Wpair, Wcoul in hResult after synchronizing.
+void device_pair_forces(System& s, bool compute);
+// P <- CP P + CF F (free atoms); optional 2KE per dimension into hResult[10..12].
+void device_boost(System& s, double CP, double CF, bool kinetic);
+// R <- CR R + CP P / m (free atoms).
+void device_move(System& s, double CR, double CP);
+void device_pair_statistics(System& s, long* listed, long* within);
+// Neighbor pairs (1-based, i<j) of the current lists.
+long device_neighbor_pairs(System& s, int* pairs, long capacity);
+
+}  // namespace emdee

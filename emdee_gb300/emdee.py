@@ -103,7 +103,17 @@ SIGNATURES = {
     "EmDee_set_precision": (None, [tEmDee, _I]),
     "EmDee_neighbor_pairs": (C.c_long, [tEmDee, _P, C.c_long]),
     "EmDee_destroy": (None, [_PT]),
+    "EmDee_cuda_stream": (_P, [tEmDee]),
+    "EmDee_profile": (None, [tEmDee, _I]),
+    "EmDee_kernel_times": (_I, [tEmDee, _P, _P, _I]),
+    "EmDee_pair_statistics": (None, [tEmDee, _P, _P]),
+    "EmDee_launch_count": (C.c_long, [tEmDee]),
 }
+
+# entry points of the GB300 library with no counterpart in the reference
+EXTENSIONS = {"EmDee_set_precision", "EmDee_neighbor_pairs", "EmDee_destroy", "EmDee_cuda_stream",
+              "EmDee_profile", "EmDee_kernel_times", "EmDee_pair_statistics",
+              "EmDee_launch_count"}
 
 MIXED, FP64 = 0, 1
 
@@ -122,6 +132,8 @@ class EmDee:
         self.path = path
         self.lib = C.CDLL(path, mode=C.RTLD_LOCAL)
         for name, (res, args) in SIGNATURES.items():
+            if name in EXTENSIONS and not hasattr(self.lib, name):
+                continue
             fn = getattr(self.lib, name)
             fn.restype = res
             fn.argtypes = args

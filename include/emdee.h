@@ -222,6 +222,26 @@ void EmDee_set_precision(tEmDee md, int mode);
  * capacity is too small.  Used to compare pair sets with the reference. */
 long EmDee_neighbor_pairs(tEmDee md, int* pairs, long capacity);
 
+/* The cudaStream_t on which the system's kernels run (for CUDA-event timing
+ * by the caller). */
+void* EmDee_cuda_stream(tEmDee md);
+
+/* Turns per-kernel CUDA-event timing on (1) or off (0). */
+void EmDee_profile(tEmDee md, int on);
+
+/* Accumulated device time (ms) and launch counts per kernel class since the
+ * last call: [0] skin check, [1] list build, [2] position packing, [3] pair
+ * forces, [4] boost, [5] move.  Writes min(n, 6) entries, resets them and
+ * returns 6. */
+int EmDee_kernel_times(tEmDee md, double* ms, long* launches, int n);
+
+/* Half-list statistics: pairs in the current neighbor lists and pairs within
+ * the cut-off at the last force evaluation. */
+void EmDee_pair_statistics(tEmDee md, long* listed, long* within);
+
+/* Number of CUDA kernels the library has launched for this system. */
+long EmDee_launch_count(tEmDee md);
+
 /* Releases the system and its device memory (the reference has no destroy). */
 void EmDee_destroy(tEmDee* md);
 
