@@ -455,16 +455,6 @@ static void grow(T*& p, size_t& have, size_t need) {
   have = need;
 }
 
-struct GridCaps {
-  size_t ranks = 0, atoms = 0, tiles = 0, nb = 0, scan = 0;
-};
-static GridCaps& caps_of(System& s) {
-  static std::vector<std::pair<System*, GridCaps>> all;
-  for (auto& p : all)
-    if (p.first == &s) return p.second;
-  all.push_back({&s, GridCaps()});
-  return all.back().second;
-}
 
 static size_t build_smem(const Grid& g, int ntypes) {
   return (size_t)(g.maxHalo + 1) * (sizeof(float4) + sizeof(int) + 1) + 3 * sizeof(int) * (g.haloCells + 1) +
@@ -483,7 +473,7 @@ static int choose_tile(int M, double perCell) {
 // src/neighbor_lists.f90:175-195 (build part) and 199-300
 void device_build_lists(System& s) {
   Grid& g = s.grid;
-  GridCaps& c = caps_of(s);
+  GridCaps& c = g.caps;
   const int N = s.natoms;
   prof_begin(s, PK_BUILD);
   const double L = *s.Lbox;

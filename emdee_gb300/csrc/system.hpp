@@ -71,6 +71,10 @@ struct Kiss {
 
 // ---- neighbor machinery ------------------------------------------------------
 
+struct GridCaps {   // allocated capacities of the grid arrays
+  size_t ranks = 0, atoms = 0, tiles = 0, nb = 0, scan = 0;
+};
+
 struct Grid {
   int M = 0;            // cells per dimension (src/neighbor_lists.f90:185-186)
   int TB = 0;           // tile edge in cells
@@ -93,6 +97,7 @@ struct Grid {
   int* dTileInfo = nullptr;   // per tile: atoms, halo atoms
   int2* dHaloTab = nullptr;   // per tile and halo cell: rank, packed halo coordinates
   size_t haloTabCap = 0;
+  GridCaps caps;
 };
 
 struct DevModels {   // per-layer pair tables uploaded for the kernels

@@ -124,3 +124,14 @@ def test_trajectory_fp64_tracks_oracle(gpu, oracle):
     Ro = oracle.download(ref, "coordinates", (N, 3))
     Rd = gpu.download(dev, "coordinates", (N, 3))
     assert np.max(np.abs(Ro - Rd)) < 1e-9
+
+
+def test_destroy_and_recreate(gpu, oracle):
+    """A system created after another was destroyed starts from clean state."""
+    ref = _fcc_system(oracle, 2048, 0.8, 9, None)
+    Fo = oracle.download(ref, "forces", (2048, 3))
+    for _ in range(3):
+        md = _fcc_system(gpu, 2048, 0.8, 9, MIXED)
+        F = gpu.download(md, "forces", (2048, 3))
+        assert rel_rms(F, Fo) < FORCE_RMS_MIXED
+        gpu.EmDee_destroy(C.byref(md))
