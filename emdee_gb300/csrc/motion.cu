@@ -149,4 +149,83 @@ void device_pair_statistics(System& s, long* listed, long* within) {
   if (within) *within = (long)(w + 0.5);
 }
 
+// ---------------------------------------------------------------------------------
+// EmDee_boost_noalloc: the boost + kinetic-energy kernel on caller-owned device
+// arrays, with its scratch in a fixed device array instead of cudaMalloc.
+//
+// Who needs it: callers that must not allocate device memory at this point,
+// such as code running in a cudaLaunchHostFunc callback (CUDA calls that
+// allocate are not permitted there), loops that cannot afford the device-wide
+// synchronization that cudaMalloc/cudaFree may imply, and processes whose
+// device memory is entirely reserved by another allocator.
+//
+// The scratch holds one partial sum per thread block (3 doubles) and the
+// completion ticket of the grid reduction.  It lives in every GPU that loads
+// this library until the process exits.  All calls share it: calls that
+// overlap on the GPU (different streams, different host threads) race, so
+// serialize them.  The first call on each device looks up the array's device
+// address (cudaGetSymbolAddress); make that first call before any stream
+// capture.
+// ---------------------------------------------------------------------------------
+
+namespace {
+
+const int NOALLOC_MAX_BLOCKS = 1184;   // the grid size cap of device_boost
+const long long NOALLOC_MAX_ATOMS = 715827882LL;   // 3N must fit in a signed 32-bit index
+// [0, 3*MAX_BLOCKS) per-block partial sums; [3*MAX_BLOCKS] ticket (as 8 bytes)
+static __device__ __align__(256) double g_noalloc_scratch[3 * NOALLOC_MAX_BLOCKS + 1];
+
+void* noalloc_scratch_address() {
+  static void* addr[64] = {nullptr};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  if (!addr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) {
+      fprintf(stderr, "Error in boost_noalloc: cannot locate the scratch array on device %d (%s).\n", dev,
+              cudaGetErrorString(e));
+      return nullptr;
+    }
+    addr[dev] = p;
+  }
+  return addr[dev];
+}
+
+}  // namespace
+
 }  // namespace emdee
+
+// P <- CP P + CF F for N atoms (device arrays double[N][3]) and, in twoKE
+// (device double[3]), 2KE per dimension = sum over atoms of P^2/m with the
+// updated momenta.  invMass is a device double[N] array, or NULL for unit
+// masses.  Returns 0 on success, 1 for a size outside [1, 715827882] atoms,
+// 2 for a CUDA error; the reason is printed on stderr.  Allocates no memory.
+extern "C" int EmDee_boost_noalloc(double* P, const double* F, const double* invMass, int N, double CP, double CF,
+                                   double* twoKE, void* stream) {
+  using namespace emdee;
+  if (N < 1 || (long long)N > NOALLOC_MAX_ATOMS) {
+    fprintf(stderr, "Error in boost_noalloc: %d atoms is outside the supported range [1, %lld].\n", N,
+            NOALLOC_MAX_ATOMS);
+    return 1;
+  }
+  double* scratch = (double*)noalloc_scratch_address();
+  if (!scratch) return 2;
+  cudaStream_t st = (cudaStream_t)stream;
+  unsigned int* ticket = (unsigned int*)(scratch + 3 * NOALLOC_MAX_BLOCKS);
+  // the ticket must start at zero; partial sums are overwritten before use
+  cudaError_t e = cudaMemsetAsync(ticket, 0, sizeof(unsigned int), st);
+  int blocks = motion_blocks(N);
+  bool unitCP = CP == 1.0, unitM = invMass == nullptr;
+  auto kern = unitCP ? (unitM ? k_boost<true, true, true> : k_boost<true, true, false>)
+                     : (unitM ? k_boost<true, false, true> : k_boost<true, false, false>);
+  if (e == cudaSuccess) {
+    kern<<<blocks, MOTION_THREADS, 0, st>>>(P, F, invMass, N, CP, CF, scratch, ticket, twoKE - 10);
+    e = cudaGetLastError();
+  }
+  if (e != cudaSuccess) {
+    fprintf(stderr, "Error in boost_noalloc: %s.\n", cudaGetErrorString(e));
+    return 2;
+  }
+  return 0;
+}

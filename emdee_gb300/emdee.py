@@ -108,12 +108,13 @@ SIGNATURES = {
     "EmDee_kernel_times": (_I, [tEmDee, _P, _P, _I]),
     "EmDee_pair_statistics": (None, [tEmDee, _P, _P]),
     "EmDee_launch_count": (C.c_long, [tEmDee]),
+    "EmDee_boost_noalloc": (C.c_int, [_P, _P, _P, _I, _D, _D, _P, _P]),
 }
 
 # entry points of the GB300 library with no counterpart in the reference
 EXTENSIONS = {"EmDee_set_precision", "EmDee_neighbor_pairs", "EmDee_destroy", "EmDee_cuda_stream",
               "EmDee_profile", "EmDee_kernel_times", "EmDee_pair_statistics",
-              "EmDee_launch_count"}
+              "EmDee_launch_count", "EmDee_boost_noalloc"}
 
 MIXED, FP64 = 0, 1
 

@@ -242,6 +242,22 @@ void EmDee_pair_statistics(tEmDee md, long* listed, long* within);
 /* Number of CUDA kernels the library has launched for this system. */
 long EmDee_launch_count(tEmDee md);
 
+/* No counterpart in the reference.  EmDee_boost's momentum update and
+ * kinetic-energy sums on caller-owned device arrays, allocating nothing: for
+ * callers that cannot call cudaMalloc at that point (inside a
+ * cudaLaunchHostFunc callback, in loops that cannot afford the synchronization
+ * cudaMalloc/cudaFree may imply, or when another allocator owns the device
+ * memory).  P (double[N][3], updated in place), F (double[N][3]), invMass
+ * (double[N], or NULL for unit masses) and twoKE (double[3]: 2KE per
+ * dimension) are device pointers; stream is a cudaStream_t (NULL: default).
+ * The reduction scratch is a fixed 28 KB device array held by every GPU that
+ * loads the library until exit and shared by all calls: calls that overlap on
+ * the GPU race.  The first call on a device looks up that array's address; make
+ * it before any stream capture.  N must lie in [1, 715827882].  Returns 0, 1 for
+ * a size out of range, 2 for a CUDA error (reason on stderr). */
+int EmDee_boost_noalloc(double* P, const double* F, const double* invMass, int N, double CP, double CF,
+                        double* twoKE, void* stream);
+
 /* Releases the system and its device memory (the reference has no destroy). */
 void EmDee_destroy(tEmDee* md);
 
