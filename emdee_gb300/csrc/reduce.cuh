@@ -67,18 +67,32 @@ __device__ __forceinline__ void grid_reduce(double (&v)[NQ], double* partials, u
   grid_reduce_lane0<NQ, THREADS>(v, partials, ticket, result);
 }
 
-// Warp sum of FP32 values with an error-free two-sum at every level; lane 0
-// returns hi + lo in FP64.
-__device__ __forceinline__ double warp_sum_f32(float x) {
-  float hi = x, lo = 0.f;
+// Warp sums of FP32 values with an error-free two-sum at every level; lane 0
+// converts hi + lo to FP64 (other lanes return 0 and touch no FP64 unit).
+template <int NQ>
+__device__ __forceinline__ void warp_sum_f32(const float (&x)[NQ], double (&out)[NQ]) {
+  float hi[NQ], lo[NQ];
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    float h2 = __shfl_down_sync(0xffffffffu, hi, o), l2 = __shfl_down_sync(0xffffffffu, lo, o);
-    float s = hi + h2, bp = s - hi, err = (hi - (s - bp)) + (h2 - bp);
-    hi = s;
-    lo = lo + l2 + err;
+  for (int q = 0; q < NQ; q++) {
+    hi[q] = x[q];
+    lo[q] = 0.f;
   }
-  return (double)hi + (double)lo;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int q = 0; q < NQ; q++) {
+      float h2 = __shfl_down_sync(0xffffffffu, hi[q], o), l2 = __shfl_down_sync(0xffffffffu, lo[q], o);
+      float s = hi[q] + h2, bp = s - hi[q], err = (hi[q] - (s - bp)) + (h2 - bp);
+      hi[q] = s;
+      lo[q] = lo[q] + l2 + err;
+    }
+  if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+    for (int q = 0; q < NQ; q++) out[q] = (double)hi[q] + (double)lo[q];
+  } else {
+#pragma unroll
+    for (int q = 0; q < NQ; q++) out[q] = 0.0;
+  }
 }
 
 // grid_reduce for per-thread FP32 partial sums: compensated warp sums in FP32,
@@ -87,8 +101,7 @@ template <int NQ, int THREADS>
 __device__ __forceinline__ void grid_reduce_f32(const float (&v)[NQ], double* partials, unsigned int* ticket,
                                                 double* result) {
   double w[NQ];
-#pragma unroll
-  for (int q = 0; q < NQ; q++) w[q] = warp_sum_f32(v[q]);
+  warp_sum_f32<NQ>(v, w);
   grid_reduce_lane0<NQ, THREADS>(w, partials, ticket, result);
 }
 

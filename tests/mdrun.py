@@ -70,3 +70,50 @@ def fcc_lattice(N, L, jitter, seed):
     sites = (g[:, None, :] + base[None, :, :]).reshape(-1, 3)[:N] * a
     rng = np.random.default_rng(seed)
     return sites + rng.uniform(-jitter, jitter, size=sites.shape)
+
+
+COUL_MODELS = {
+    # name -> factory(lib) as the reference's test_coul_*.f90 build them (test/test_coul_*.f90:45)
+    "coul_cut": lambda lib: lib.EmDee_coul_cut(),
+    "coul_sf": lambda lib: lib.EmDee_coul_sf(),
+    "coul_damped": lambda lib: lib.EmDee_coul_damped(0.2),
+    "coul_damped_smoothed": lambda lib: lib.EmDee_coul_damped_smoothed(0.2, 1.0),
+    "coul_damped_square_smoothed": lambda lib: lib.EmDee_coul_damped_square_smoothed(0.2, 1.0),
+    "coul_square_smoothed": lambda lib: lib.EmDee_coul_square_smoothed(1.0),
+    "coul_shifted_square_smoothed": lambda lib: lib.EmDee_coul_shifted_square_smoothed(1.0),
+    "shifted_force(coul_damped)": lambda lib: lib.EmDee_shifted_force(lib.EmDee_coul_damped(0.2)),
+    "square_smoothed(coul_cut)": lambda lib: lib.EmDee_square_smoothed(lib.EmDee_coul_cut(), 1.0),
+}
+
+
+def setup_water(lib, cfg, coul, pair="shifted_force", precision=None, natoms=None, exclusions=True):
+    """SPC/E sample as free atoms (test/test_coul_*.f90:33-48 without rigid bodies):
+    O-O Lennard-Jones (H: pair_none), the Coulomb model `coul`, intramolecular
+    pairs excluded with EmDee_ignore_pair."""
+    run = cfg["run"]
+    N = natoms or len(cfg["coordinates"])
+    md = lib.system(1, 1, run["Rc"], run["skin"], N, cfg["type"][:N], cfg["mass"])
+    if precision is not None:
+        lib.EmDee_set_precision(md, precision)
+    for i, (eps, sig) in enumerate(zip(cfg["epsilon"], cfg["sigma"])):
+        if eps == 0.0:
+            p = lib.EmDee_pair_none()
+        elif pair == "softcore":
+            p = lib.EmDee_pair_softcore_cut(eps / run["mvv2e"], sig, 0.7)
+        else:
+            p = lib.EmDee_shifted_force(lib.EmDee_pair_lj_cut(eps / run["mvv2e"], sig))
+        lib.EmDee_set_pair_model(md, i + 1, i + 1, p, run["kCoul"])
+    lib.EmDee_set_coul_model(md, COUL_MODELS[coul](lib))
+    if exclusions:
+        mol = cfg["molecule"][:N]
+        first = {}
+        for a, m in enumerate(mol):
+            first.setdefault(m, []).append(a + 1)
+        for atoms in first.values():
+            for x in range(len(atoms)):
+                for y in range(x + 1, len(atoms)):
+                    lib.EmDee_ignore_pair(md, atoms[x], atoms[y])
+    lib.upload(md, "charges", cfg["charge"][:N])
+    lib.upload(md, "box", np.array([cfg["box"]]))
+    lib.upload(md, "coordinates", np.array(cfg["coordinates"][:N]))
+    return md
