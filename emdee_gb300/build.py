@@ -29,8 +29,9 @@ UNITS = {
     "pair_fp64.cu": ["-fmad=false"],
     "motion.cu": ["-fmad=false"],
     "pair_mixed.cu": [],
+    "bodies.cu": ["-fmad=false"],
 }
-HEADERS = ["system.hpp", "pairmath.cuh", "tile.cuh", "reduce.cuh", os.path.join("..", "..", "include", "emdee.h")]
+HEADERS = ["system.hpp", "pairmath.cuh", "tile.cuh", "reduce.cuh", "rigid.cuh", os.path.join("..", "..", "include", "emdee.h")]
 
 
 def _stale(target, deps):

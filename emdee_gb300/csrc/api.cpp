@@ -244,8 +244,10 @@ static void compute_forces_impl(tEmDee* md);
 
 static void initialize_system(tEmDee* md) {   // src/EmDeeCode.f90:916-923 and src/EmDeeData.f90:359-416
   System& s = *sys_of(*md);
-  md->RotDoF = 0;
-  md->DoF = 3 * s.nfree - 3;
+  bodies_update(s);
+  int bodyDoF = 6 * s.nbodies;
+  md->RotDoF = bodyDoF - 3 * s.nbodies;
+  md->DoF = 3 * s.nfree + bodyDoF - 3;
   check_actual_interactions(s);
   bool need = false;
   for (int l = 0; l < s.nlayers; l++) need |= s.coul[l].requires_kspace != 0;
@@ -283,6 +285,10 @@ static void compute_forces_impl(tEmDee* md) {
   const double* r = s.hResult;   // Epair, Ecoul, Wpair, Wcoul
   md->Virial.Total = r[2] + r[3] + 0.0 + 0.0 + 0.0;
   md->Virial.Body = 0.0;
+  if (s.nbodies != 0) {   // src/EmDeeData.f90:926-953
+    md->Virial.Body = bodies_virial(s);
+    md->Virial.Total = md->Virial.Total + md->Virial.Body;
+  }
   if (compute) {
     md->Energy.Dispersion = r[0];
     md->Energy.Coulomb = r[1] + 0.0;
@@ -359,18 +365,73 @@ tEmDee EmDee_system(int threads, int layers, double rc, double skin, int N, int*
   s->charge.assign(N, 0.0);
   s->charged.assign(N, 0);
 
-  // rigid bodies (src/EmDeeData.f90:268-355): free atoms get distinct body ids
+  // rigid bodies (src/EmDeeData.f90:268-355): entries <= 0 or unique are free
+  // atoms; other values are renumbered 1..nbodies in order of first appearance
+  s->atomBody.assign(N, 0);
   if (bodies) {
-    std::vector<int> seen;
+    std::vector<int> saved, amount, first;
+    for (int i = 0; i < N; i++) {
+      int ib = bodies[i], j = -1;
+      if (ib <= 0) continue;
+      for (size_t k = 0; k < saved.size(); k++)
+        if (saved[k] == ib) { j = (int)k; break; }
+      if (j < 0) {
+        saved.push_back(ib);
+        amount.push_back(1);
+        first.push_back(i);
+      } else {
+        amount[j]++;
+        s->atomBody[i] = j + 1;
+        s->atomBody[first[j]] = j + 1;
+      }
+    }
+    int k = 0;
+    for (size_t j = 0; j < saved.size(); j++)
+      if (amount[j] > 1) saved[j] = ++k;
     for (int i = 0; i < N; i++)
-      if (bodies[i] > 0)
-        for (int j = i + 1; j < N; j++)
-          if (bodies[j] == bodies[i]) fatal("system setup", "rigid bodies are not available in this build");
+      if (s->atomBody[i] > 0) s->atomBody[i] = saved[s->atomBody[i] - 1];
+    s->nbodies = k;
   }
-  s->nbodies = 0;
-  s->nfree = N;
-  s->atomBody.resize(N);
-  for (int i = 0; i < N; i++) s->atomBody[i] = i + 1;
+  for (int i = 0; i < N; i++)
+    if (s->atomBody[i] == 0) s->freeList.push_back(i);
+  s->nfree = (int)s->freeList.size();
+  if (s->nbodies > 0) {
+    std::vector<int> cnt(s->nbodies, 0);
+    for (int i = 0; i < N; i++)
+      if (s->atomBody[i] > 0) cnt[s->atomBody[i] - 1]++;
+    s->hBodies.assign(s->nbodies, BodyState());
+    int off = 0;
+    for (int b = 0; b < s->nbodies; b++) {
+      BodyState& B = s->hBodies[b];
+      memset(&B, 0, sizeof(BodyState));
+      B.first = off;
+      B.NP = 0;
+      B.dof = 6;
+      off += cnt[b];
+    }
+    s->hBodyAtom.assign(off, 0);
+    s->hBodyM.assign(off, 0.0);
+    s->hBodyD.assign((size_t)3 * off, 0.0);
+    s->hBodyDelta.assign((size_t)3 * off, 0.0);
+    for (int i = 0; i < N; i++)
+      if (s->atomBody[i] > 0) {
+        BodyState& B = s->hBodies[s->atomBody[i] - 1];
+        s->hBodyAtom[B.first + B.NP] = i;
+        s->hBodyM[B.first + B.NP] = s->mass[i];
+        B.NP++;
+      }
+    for (int b = 0; b < s->nbodies; b++) {
+      BodyState& B = s->hBodies[b];
+      B.mass = 0.0;
+      for (int j = 0; j < B.NP; j++) B.mass += s->hBodyM[B.first + j];
+      B.invMass = 1.0 / B.mass;
+    }
+  }
+  {
+    int k = s->nbodies;   // free atoms get distinct body indices
+    for (int i = 0; i < N; i++)
+      if (s->atomBody[i] == 0) s->atomBody[i] = ++k;
+  }
 
   s->exFirst.assign(N, 1);
   s->exLast.assign(N, 0);
@@ -409,11 +470,26 @@ tEmDee EmDee_system(int threads, int layers, double rc, double skin, int N, int*
   CK(cudaMemset(s->dCharge, 0, sizeof(double) * N));
   CK(cudaMemcpy(s->dType, s->atomType.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(s->dBody, s->atomBody.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
-  CK(cudaMallocHost(&s->hResult, sizeof(double) * 16));
-  CK(cudaMalloc(&s->dResult, sizeof(double) * 16));
+  if (s->nbodies > 0) {
+    size_t na = s->hBodyAtom.size();
+    CK(cudaMalloc(&s->dBodies, sizeof(BodyState) * s->nbodies));
+    CK(cudaMalloc(&s->dBodyAtom, sizeof(int) * na));
+    CK(cudaMalloc(&s->dBodyM, sizeof(double) * na));
+    CK(cudaMalloc(&s->dBodyD, sizeof(double) * 3 * na));
+    CK(cudaMalloc(&s->dBodyDelta, sizeof(double) * 3 * na));
+    CK(cudaMemcpy(s->dBodies, s->hBodies.data(), sizeof(BodyState) * s->nbodies, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s->dBodyAtom, s->hBodyAtom.data(), sizeof(int) * na, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s->dBodyM, s->hBodyM.data(), sizeof(double) * na, cudaMemcpyHostToDevice));
+    CK(cudaMemset(s->dBodyD, 0, sizeof(double) * 3 * na));
+    CK(cudaMemset(s->dBodyDelta, 0, sizeof(double) * 3 * na));
+    CK(cudaMalloc(&s->dFree, sizeof(int) * (s->nfree > 0 ? s->nfree : 1)));
+    if (s->nfree > 0) CK(cudaMemcpy(s->dFree, s->freeList.data(), sizeof(int) * s->nfree, cudaMemcpyHostToDevice));
+  }
+  CK(cudaMallocHost(&s->hResult, sizeof(double) * 24));
+  CK(cudaMalloc(&s->dResult, sizeof(double) * 24));
   CK(cudaMalloc(&s->dTicket, sizeof(unsigned int) * 4));
   CK(cudaMemset(s->dTicket, 0, sizeof(unsigned int) * 4));
-  memset(s->hResult, 0, sizeof(double) * 16);
+  memset(s->hResult, 0, sizeof(double) * 24);
 
   md.Builds = 0;
   md.DoF = 3 * (N - 1);
@@ -447,6 +523,15 @@ void EmDee_destroy(tEmDee* md) {
   cudaFree(s->dCharge);
   cudaFree(s->dType);
   cudaFree(s->dBody);
+  if (s->ownsBodies) {
+    cudaFree(s->dBodies);
+    cudaFree(s->dBodyDelta);
+  }
+  cudaFree(s->dBodyAtom);
+  cudaFree(s->dBodyM);
+  cudaFree(s->dBodyD);
+  cudaFree(s->dFree);
+  cudaFree(s->dBodyScratch);
   cudaFree(s->dExFirst);
   cudaFree(s->dExCount);
   cudaFree(s->dExItem);
@@ -662,23 +747,36 @@ void EmDee_upload(tEmDee* md, char* option, double* address) {
     CK(cudaMemcpyAsync(s.dR, address, sizeof(double) * n3, cudaMemcpyHostToDevice, s.stream));
     if (s.hMirrorR) memcpy(s.hMirrorR, address, sizeof(double) * n3);
     s.hasR = true;
-    if (s.initialized) mark_stale(s, md);
-    else if (s.Lbox) initialize_system(md);
+    if (s.initialized) {
+      mark_stale(s, md);
+      if (md->Options.AutoBodyUpdate) bodies_update(s);
+    } else if (s.Lbox) {
+      initialize_system(md);
+    }
   } else if (!strcmp(item, "momenta")) {
     if (!s.initialized) fatal("upload", "box and coordinates have not been defined");
     CK(cudaMemcpyAsync(s.dP, address, sizeof(double) * n3, cudaMemcpyHostToDevice, s.stream));
     if (s.hMirrorP) memcpy(s.hMirrorP, address, sizeof(double) * n3);
-    double t2[3] = {0, 0, 0};   // src/EmDeeData.f90:157-189 (free atoms)
-    for (int i = 0; i < s.natoms; i++)
+    double t2[3] = {0, 0, 0}, r2[3] = {0, 0, 0};   // src/EmDeeData.f90:157-189
+    for (int i : s.freeList)
       for (int d = 0; d < 3; d++) t2[d] += s.invMass[i] * (address[3 * i + d] * address[3 * i + d]);
+    if (s.nbodies > 0) {
+      double k6[6];
+      bodies_assign(s, k6);
+      for (int d = 0; d < 3; d++) {
+        t2[d] += k6[d];
+        r2[d] = k6[3 + d];
+      }
+    }
     for (int d = 0; d < 3; d++) {
-      md->Kinetic.RotPart[d] = 0.0;
+      md->Kinetic.RotPart[d] = 0.5 * r2[d];
       md->Kinetic.TransPart[d] = 0.5 * t2[d];
     }
-    md->Kinetic.Rotational = 0.0;
-    md->Kinetic.Total = md->Kinetic.TransPart[0] + md->Kinetic.TransPart[1] + md->Kinetic.TransPart[2] + 0.0;
+    md->Kinetic.Rotational = md->Kinetic.RotPart[0] + md->Kinetic.RotPart[1] + md->Kinetic.RotPart[2];
+    md->Kinetic.Total = md->Kinetic.TransPart[0] + md->Kinetic.TransPart[1] + md->Kinetic.TransPart[2] +
+                        md->Kinetic.Rotational;
     md->Kinetic.ShadowKinetic = md->Kinetic.Total;
-    md->Kinetic.ShadowRotational = 0.0;
+    md->Kinetic.ShadowRotational = md->Kinetic.Rotational;
     md->Kinetic.UpToDate = true;
   } else if (!strcmp(item, "forces")) {
     if (!s.initialized) fatal("upload", "box and coordinates have not been defined");
@@ -708,11 +806,50 @@ void EmDee_download(tEmDee md, char* option, double* address) {
   MirrorScope scope(s);
   if (!strcmp(item, "box")) {
     *address = *s.Lbox;
-  } else if (!strcmp(item, "coordinates") || !strcmp(item, "centersOfMass")) {
+  } else if (!strcmp(item, "coordinates")) {
     if (!s.hasR) fatal("download", "coordinates have not been allocated");
     CK(cudaMemcpyAsync(address, s.dR, b, cudaMemcpyDeviceToHost, s.stream));
   } else if (!strcmp(item, "momenta")) {
-    CK(cudaMemcpyAsync(address, s.dP, b, cudaMemcpyDeviceToHost, s.stream));
+    if (s.nbodies == 0) {
+      CK(cudaMemcpyAsync(address, s.dP, b, cudaMemcpyDeviceToHost, s.stream));
+    } else {   // free atoms: P; body atoms: particle momenta (src/EmDeeCode.f90:729-741)
+      double* tmp;
+      CK(cudaMalloc(&tmp, b));
+      CK(cudaMemcpyAsync(tmp, s.dP, b, cudaMemcpyDeviceToDevice, s.stream));
+      bodies_particle_momenta(s, tmp);
+      CK(cudaMemcpyAsync(address, tmp, b, cudaMemcpyDeviceToHost, s.stream));
+      CK(cudaStreamSynchronize(s.stream));
+      CK(cudaFree(tmp));
+    }
+  } else if (!strcmp(item, "centersOfMass")) {   // bodies first, then free atoms
+    std::vector<double> R((size_t)3 * s.natoms);
+    CK(cudaMemcpyAsync(R.data(), s.dR, b, cudaMemcpyDeviceToHost, s.stream));
+    bodies_download(s);
+    for (int k = 0; k < s.nbodies; k++)
+      for (int d = 0; d < 3; d++) address[3 * k + d] = s.hBodies[k].rcm[d];
+    for (int j = 0; j < s.nfree; j++)
+      for (int d = 0; d < 3; d++) address[3 * (s.nbodies + j) + d] = R[3 * s.freeList[j] + d];
+  } else if (!strcmp(item, "quaternions") || !strcmp(item, "quatmom") || !strcmp(item, "quattau")) {
+    bodies_download(s);
+    for (int k = 0; k < s.nbodies; k++) {
+      const BodyState& B = s.hBodies[k];
+      if (!strcmp(item, "quaternions")) for (int d = 0; d < 4; d++) address[4 * k + d] = B.q[d];
+      else if (!strcmp(item, "quatmom")) for (int d = 0; d < 4; d++) address[4 * k + d] = B.pi[d];
+      else {
+        double v[3] = {2.0 * B.tau[0], 2.0 * B.tau[1], 2.0 * B.tau[2]};
+        rb_C(B.q, v, &address[4 * k]);
+      }
+    }
+  } else if (!strcmp(item, "angmom") || !strcmp(item, "bodycoord") || !strcmp(item, "bodymom") ||
+             !strcmp(item, "bodyforces") || !strcmp(item, "torques") || !strcmp(item, "inertia")) {
+    bodies_download(s);
+    for (int k = 0; k < s.nbodies; k++) {
+      const BodyState& B = s.hBodies[k];
+      const double* v = !strcmp(item, "angmom") ? B.omega : !strcmp(item, "bodycoord") ? B.rcm :
+                        !strcmp(item, "bodymom") ? B.pcm : !strcmp(item, "bodyforces") ? B.F :
+                        !strcmp(item, "torques") ? B.tau : B.MoI;
+      for (int d = 0; d < 3; d++) address[3 * k + d] = v[d];
+    }
   } else if (!strcmp(item, "forces")) {
     if (!s.forcesUpToDate[s.layer - 1]) compute_forces_impl(&md);
     CK(cudaMemcpyAsync(address, s.F(), b, cudaMemcpyDeviceToHost, s.stream));
@@ -770,6 +907,15 @@ void EmDee_share_phase_space(tEmDee mdkeep, tEmDee* mdlose) {
   lose.dR = keep.dR;
   lose.dP = keep.dP;
   lose.ownsRP = false;
+  if (lose.nbodies > 0) {   // the reference aliases the body array as well
+    if (lose.ownsBodies) {
+      CK(cudaFree(lose.dBodies));
+      CK(cudaFree(lose.dBodyDelta));
+    }
+    lose.dBodies = keep.dBodies;
+    lose.dBodyDelta = keep.dBodyDelta;
+    lose.ownsBodies = false;
+  }
   if (lose.ownsLbox) delete lose.Lbox;
   lose.Lbox = keep.Lbox;
   lose.ownsLbox = false;
@@ -799,9 +945,29 @@ void EmDee_random_momenta(tEmDee* md, double kT, bool adjust, int seed) {
   MirrorScope scope(s);
   int N = s.natoms;
   std::vector<double> P((size_t)3 * N, 0.0);
-  double twoKEt[3] = {0, 0, 0};
+  double twoKEt[3] = {0, 0, 0}, twoKEr[3] = {0, 0, 0};
   if (s.random.seeding_required) s.random.setup(seed);
-  for (int i = 0; i < N; i++) {
+  if (s.nbodies != 0) {
+    if (!s.initialized) fatal("random_momenta", "coordinates have not defined");
+    bodies_download(s);
+    for (BodyState& b : s.hBodies) {
+      double f = std::sqrt(b.mass * kT), w[3];
+      double a0 = s.random.normal(), a1 = s.random.normal(), a2 = s.random.normal();
+      b.pcm[0] = f * a0;
+      b.pcm[1] = f * a1;
+      b.pcm[2] = f * a2;
+      double c0 = s.random.normal(), c1 = s.random.normal(), c2 = s.random.normal();
+      w[0] = std::sqrt(b.invMoI[0] * kT) * c0;
+      w[1] = std::sqrt(b.invMoI[1] * kT) * c1;
+      w[2] = std::sqrt(b.invMoI[2] * kT) * c2;
+      rb_assign_omega(b, w);
+      for (int d = 0; d < 3; d++) {
+        twoKEt[d] += b.invMass * (b.pcm[d] * b.pcm[d]);
+        twoKEr[d] += b.MoI[d] * (b.omega[d] * b.omega[d]);
+      }
+    }
+  }
+  for (int i : s.freeList) {
     double f = std::sqrt(s.mass[i] * kT);
     double a = s.random.normal(), b = s.random.normal(), c = s.random.normal();
     P[3 * i] = f * a;
@@ -809,35 +975,52 @@ void EmDee_random_momenta(tEmDee* md, double kT, bool adjust, int seed) {
     P[3 * i + 2] = f * c;
     for (int d = 0; d < 3; d++) twoKEt[d] += s.invMass[i] * (P[3 * i + d] * P[3 * i + d]);
   }
-  if (adjust) {
+  if (adjust) {   // src/EmDeeCode.f90:994-1018
     double vcm[3];
     for (int d = 0; d < 3; d++) {
-      double sum = 0.0;
-      for (int i = 0; i < N; i++) sum += P[3 * i + d];
-      vcm[d] = (sum + 0.0) / s.totalMass;
+      double sum = 0.0, sb = 0.0;
+      for (int i : s.freeList) sum += P[3 * i + d];
+      for (const BodyState& b : s.hBodies) sb += b.pcm[d];
+      vcm[d] = (sum + sb) / s.totalMass;
       twoKEt[d] = 0.0;
     }
-    for (int i = 0; i < N; i++)
+    for (int i : s.freeList)
       for (int d = 0; d < 3; d++) {
         P[3 * i + d] = P[3 * i + d] - s.mass[i] * vcm[d];
         twoKEt[d] += s.invMass[i] * (P[3 * i + d] * P[3 * i + d]);
       }
-    double sum = (twoKEt[0] + 0.0) + (twoKEt[1] + 0.0) + (twoKEt[2] + 0.0);
-    double factor = std::sqrt((double)(3 * s.nfree + 0 - 3) * kT / sum);
-    for (size_t q = 0; q < P.size(); q++) P[q] *= factor;
-    for (int d = 0; d < 3; d++) twoKEt[d] = factor * factor * twoKEt[d];
+    for (BodyState& b : s.hBodies)
+      for (int d = 0; d < 3; d++) {
+        b.pcm[d] = b.pcm[d] - b.mass * vcm[d];
+        twoKEt[d] += b.invMass * (b.pcm[d] * b.pcm[d]);
+      }
+    double sum = (twoKEt[0] + twoKEr[0]) + (twoKEt[1] + twoKEr[1]) + (twoKEt[2] + twoKEr[2]);
+    double factor = std::sqrt((double)(3 * s.nfree + 6 * s.nbodies - 3) * kT / sum);
+    for (int i : s.freeList)
+      for (int d = 0; d < 3; d++) P[3 * i + d] *= factor;
+    for (BodyState& b : s.hBodies) {
+      double w[3] = {factor * b.omega[0], factor * b.omega[1], factor * b.omega[2]};
+      for (int d = 0; d < 3; d++) b.pcm[d] = factor * b.pcm[d];
+      rb_assign_omega(b, w);
+    }
+    for (int d = 0; d < 3; d++) {
+      twoKEt[d] = factor * factor * twoKEt[d];
+      twoKEr[d] = factor * factor * twoKEr[d];
+    }
   }
   CK(cudaMemcpyAsync(s.dP, P.data(), sizeof(double) * P.size(), cudaMemcpyHostToDevice, s.stream));
   CK(cudaStreamSynchronize(s.stream));
+  if (s.nbodies != 0) bodies_upload(s);
   if (s.hMirrorP) memcpy(s.hMirrorP, P.data(), sizeof(double) * P.size());
   for (int d = 0; d < 3; d++) {
-    md->Kinetic.RotPart[d] = 0.0;
+    md->Kinetic.RotPart[d] = 0.5 * twoKEr[d];
     md->Kinetic.TransPart[d] = 0.5 * twoKEt[d];
   }
-  md->Kinetic.Rotational = 0.0;
-  md->Kinetic.Total = md->Kinetic.TransPart[0] + md->Kinetic.TransPart[1] + md->Kinetic.TransPart[2] + 0.0;
+  md->Kinetic.Rotational = md->Kinetic.RotPart[0] + md->Kinetic.RotPart[1] + md->Kinetic.RotPart[2];
+  md->Kinetic.Total =
+      md->Kinetic.TransPart[0] + md->Kinetic.TransPart[1] + md->Kinetic.TransPart[2] + md->Kinetic.Rotational;
   md->Kinetic.ShadowKinetic = md->Kinetic.Total;
-  md->Kinetic.ShadowRotational = 0.0;
+  md->Kinetic.ShadowRotational = md->Kinetic.Rotational;
   md->Kinetic.UpToDate = true;
 }
 
@@ -854,14 +1037,15 @@ void EmDee_boost(tEmDee* md, double lambda, double alpha, double dt) {
   CF = lambda * CF;
   bool compute = md->Options.Compute;
   if (lambda != 0.0 && !s.forcesUpToDate[s.layer - 1]) compute_forces_impl(md);
-  bool translate = md->Options.Translate;
-  if (translate) device_boost(s, CP, CF, compute);
+  bool translate = md->Options.Translate, rotate = md->Options.Rotate;
+  if (s.nbodies > 0) bodies_boost(s, CP, CF, translate, rotate, compute);
+  else if (translate) device_boost(s, CP, CF, compute);
   if (compute) {
     if (translate)
       for (int d = 0; d < 3; d++) md->Kinetic.TransPart[d] = 0.5 * s.hResult[10 + d];
-    if (md->Options.Rotate) {
-      for (int d = 0; d < 3; d++) md->Kinetic.RotPart[d] = 0.0;
-      md->Kinetic.Rotational = 0.0;
+    if (rotate) {
+      for (int d = 0; d < 3; d++) md->Kinetic.RotPart[d] = s.nbodies > 0 ? 0.5 * s.hResult[13 + d] : 0.0;
+      md->Kinetic.Rotational = md->Kinetic.RotPart[0] + md->Kinetic.RotPart[1] + md->Kinetic.RotPart[2];
     }
     md->Kinetic.Total =
         md->Kinetic.TransPart[0] + md->Kinetic.TransPart[1] + md->Kinetic.TransPart[2] + md->Kinetic.Rotational;
@@ -883,7 +1067,8 @@ void EmDee_displace(tEmDee* md, double lambda, double alpha, double dt) {
     CR = 1.0;
   }
   CP = lambda * CP;
-  if (md->Options.Translate) device_move(s, CR, CP);
+  if (s.nbodies > 0) bodies_move(s, CR, CP, dt, md->Options.Translate, md->Options.Rotate, md->Options.RotationMode);
+  else if (md->Options.Translate) device_move(s, CR, CP);
   mark_stale(s, md);
   md->Time.Motion += wtime() - t0;
 }

@@ -22,6 +22,7 @@
 
 #include "../../include/emdee.h"
 #include "pairmath.cuh"
+#include "rigid.cuh"
 
 namespace emdee {
 
@@ -136,6 +137,16 @@ struct System {
   std::vector<char> charged;
   int nfree = 0, nbodies = 0;
   bool unitMass = true;   // every mass is exactly 1
+  // rigid bodies (src/EmDeeData.f90:268-355): host copies and device mirrors
+  std::vector<int> freeList;                  // free atoms, 0-based
+  std::vector<BodyState> hBodies;
+  std::vector<int> hBodyAtom;                 // flat atom indices of every body (0-based)
+  std::vector<double> hBodyM, hBodyD, hBodyDelta;
+  BodyState* dBodies = nullptr;
+  int *dBodyAtom = nullptr, *dFree = nullptr;
+  double *dBodyM = nullptr, *dBodyD = nullptr, *dBodyDelta = nullptr, *dBodyScratch = nullptr;
+  int bodyScratchCap = 0;
+  bool ownsBodies = true;
   std::vector<int> exFirst, exLast, exItem;   // sorted exclusion lists, 1-based items
   std::vector<PairHost> pair;                 // [layer][jtype][itype]
   std::vector<Model> coul;                    // per layer
@@ -168,7 +179,9 @@ struct System {
   int keCap = 0;
   unsigned int* dTicket = nullptr;
   // results (pinned host copy and device): [0..3] Epair, Ecoul, Wpair, Wcoul, [4] pairs within
-  // the cut-off, [8] skin value, [9] rebuild flag, [10..12] 2KE per dimension
+  // the cut-off, [6] body virial sum, [8] skin value, [9] rebuild flag, [10..12] 2KE
+  // (translational) per dimension, [13..15] 2KE (rotational), [16..21] body 2KE sums
+  // (translational, rotational) of one body kernel
   double* hResult = nullptr;
   double* dResult = nullptr;
 
@@ -205,6 +218,15 @@ void device_boost(System& s, double CP, double CF, bool kinetic);
 // R <- CR R + CP P / m (free atoms).
 void device_move(System& s, double CR, double CP);
 void device_pair_statistics(System& s, long* listed, long* within);
+// Rigid bodies (bodies.cu).
+void bodies_update(System& s);
+void bodies_boost(System& s, double CP, double CF, bool translate, bool rotate, bool kinetic);
+void bodies_move(System& s, double CR, double CP, double dt, bool translate, bool rotate, int mode);
+double bodies_virial(System& s);
+void bodies_assign(System& s, double* k6);
+void bodies_particle_momenta(System& s, double* dOut);
+void bodies_download(System& s);
+void bodies_upload(System& s);
 // Neighbor pairs (1-based, i<j) of the current lists.
 long device_neighbor_pairs(System& s, int* pairs, long capacity);
 

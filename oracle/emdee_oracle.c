@@ -34,6 +34,7 @@
 #include <omp.h>
 
 #include "../include/emdee.h"
+#include "rigid_oracle.h"
 
 #define EXTRA 2000      /* src/EmDeeData.f90:31 */
 #define NDIV 2          /* src/EmDeeData.f90:33 */
@@ -764,6 +765,8 @@ typedef struct {
   tVirial* layerVirial;
   int multilayer_coulomb;
   int ownsR;
+  obody* body;
+  int threadBodies;
 } odata;
 
 #define PAIR(me, i, j, l) ((me)->pair[((size_t)(l) * (me)->ntypes + (j)) * (me)->ntypes + (i)])
@@ -859,20 +862,80 @@ tEmDee EmDee_system(int threads, int layers, double rc, double skin, int N, int*
   me->charged = (char*)xcalloc(N, 1);
   me->atomCell = (int*)xcalloc(N, sizeof(int));
 
-  /* rigid bodies (src/EmDeeData.f90:268-355): this oracle handles free atoms */
-  me->atomBody = (int*)xmalloc(sizeof(int) * N);
+  /* rigid bodies (src/EmDeeData.f90:268-355) */
+  me->atomBody = (int*)xcalloc(N, sizeof(int));
   me->freeAtom = (int*)xmalloc(sizeof(int) * N);
-  if (bodies) {
-    for (int i = 0; i < N; i++)
-      for (int j = i + 1; j < N; j++)
-        if (bodies[i] > 0 && bodies[i] == bodies[j]) error("system setup", "rigid bodies are not handled by the oracle");
-  }
   me->nbodies = 0;
-  me->nfree = N;
-  for (int i = 0; i < N; i++) {
-    me->atomBody[i] = i + 1;
-    me->freeAtom[i] = i + 1;
+  me->nfree = 0;
+  if (bodies) {
+    /* clean_body_indices: entries <= 0 or unique are free atoms; other values
+     * are renumbered 1..nbodies in order of first appearance */
+    int *saved = (int*)xmalloc(sizeof(int) * N), *amount = (int*)xmalloc(sizeof(int) * N);
+    int *first = (int*)xmalloc(sizeof(int) * N), n = 0;
+    for (int i = 0; i < N; i++) {
+      int ib = bodies[i], j = -1;
+      me->atomBody[i] = 0;
+      if (ib <= 0) continue;
+      for (int k = 0; k < n; k++)
+        if (saved[k] == ib) { j = k; break; }
+      if (j < 0) {
+        saved[n] = ib;
+        amount[n] = 1;
+        first[n] = i;
+        n++;
+      } else {
+        amount[j]++;
+        me->atomBody[i] = j + 1;
+        me->atomBody[first[j]] = j + 1;
+      }
+    }
+    int k = 0;
+    for (int j = 0; j < n; j++)
+      if (amount[j] > 1) saved[j] = ++k;
+    for (int i = 0; i < N; i++)
+      if (me->atomBody[i] > 0) me->atomBody[i] = saved[me->atomBody[i] - 1];
+    me->nbodies = k;
+    free(saved);
+    free(amount);
+    free(first);
   }
+  for (int i = 0; i < N; i++)
+    if (me->atomBody[i] == 0) me->freeAtom[me->nfree++] = i + 1;
+  me->body = (obody*)xcalloc(me->nbodies > 0 ? me->nbodies : 1, sizeof(obody));
+  if (me->nbodies > 0) {
+    int* cnt = (int*)xcalloc(me->nbodies, sizeof(int));
+    for (int i = 0; i < N; i++)
+      if (me->atomBody[i] > 0) cnt[me->atomBody[i] - 1]++;
+    for (int b = 0; b < me->nbodies; b++) {
+      obody* B = &me->body[b];
+      B->NP = 0;
+      B->dof = 6;
+      B->index = (int*)xmalloc(sizeof(int) * cnt[b]);
+      B->M = (double*)xmalloc(sizeof(double) * cnt[b]);
+      B->d = (double*)xcalloc(3 * cnt[b], sizeof(double));
+      B->delta = (double*)xcalloc(3 * cnt[b], sizeof(double));
+    }
+    for (int i = 0; i < N; i++)
+      if (me->atomBody[i] > 0) {
+        obody* B = &me->body[me->atomBody[i] - 1];
+        B->index[B->NP] = i + 1;
+        B->M[B->NP] = me->mass[i];
+        B->NP++;
+      }
+    for (int b = 0; b < me->nbodies; b++) {
+      obody* B = &me->body[b];
+      B->mass = 0.0;
+      for (int k = 0; k < B->NP; k++) B->mass += B->M[k];
+      B->invMass = 1.0 / B->mass;
+    }
+    free(cnt);
+  }
+  {
+    int k = me->nbodies;   /* free atoms get distinct body indices */
+    for (int i = 0; i < N; i++)
+      if (me->atomBody[i] == 0) me->atomBody[i] = ++k;
+  }
+  me->threadBodies = (me->nbodies + threads - 1) / threads;
   me->threadFreeAtoms = (me->nfree + threads - 1) / threads;
 
   me->cellItem = (int*)xcalloc(N, sizeof(int));
@@ -1472,6 +1535,23 @@ void EmDee_compute_forces(tEmDee* md) {
   if (me->coul[me->layer - 1].requires_kspace) error("compute forces", "k-space electrostatics are not handled by the oracle");
   md->Virial.Total = W[0] + W[1] + W[2] + W[3] + W[4];
   md->Virial.Body = 0.0;
+  if (me->nbodies != 0) {   /* src/EmDeeData.f90:926-953 */
+    double Wb = 0.0;
+    for (int t = 0; t < nt; t++) {
+      double Wt = 0.0;
+      int b1 = t * me->threadBodies, bN = (t + 1) * me->threadBodies < me->nbodies ? (t + 1) * me->threadBodies : me->nbodies;
+      for (int b = b1; b < bN; b++) {
+        obody* B = &me->body[b];
+        double s = 0.0;
+        for (int k = 0; k < B->NP; k++)
+          for (int x = 0; x < 3; x++) s += me->F[3 * (B->index[k] - 1) + x] * B->delta[3 * k + x];
+        Wt += s;
+      }
+      Wb += Wt;
+    }
+    md->Virial.Body = -Wb;
+    md->Virial.Total = md->Virial.Total + md->Virial.Body;
+  }
   if (compute) {
     md->Energy.Dispersion = E[0];
     md->Energy.Coulomb = E[1] + E[2];
@@ -1508,9 +1588,29 @@ void EmDee_switch_model_layer(tEmDee* md, int layer) {   /* src/EmDeeCode.f90:92
 }
 
 /* src/EmDeeData.f90:359-416 (free atoms) */
+/* src/EmDeeData.f90:420-439: unwrap each body around its first atom and refresh it */
+static void update_rigid_bodies(odata* me) {
+  double L = *me->Lbox, invL = 1.0 / L;
+  for (int b = 0; b < me->nbodies; b++) {
+    obody* B = &me->body[b];
+    double* R = (double*)xmalloc(sizeof(double) * 3 * B->NP);
+    for (int k = 0; k < B->NP; k++)
+      for (int x = 0; x < 3; x++) R[3 * k + x] = me->R[3 * (B->index[k] - 1) + x];
+    for (int k = 1; k < B->NP; k++)
+      for (int x = 0; x < 3; x++) R[3 * k + x] = R[3 * k + x] - L * anint(invL * (R[3 * k + x] - R[x]));
+    body_update(B, R);
+    for (int k = 0; k < B->NP; k++)
+      for (int x = 0; x < 3; x++) me->R[3 * (B->index[k] - 1) + x] = R[3 * k + x];
+    free(R);
+  }
+}
+
 static void perform_initialization(odata* me, int* DoF, int* RotDoF) {
-  *RotDoF = 0;
-  *DoF = 3 * me->nfree - 3;
+  update_rigid_bodies(me);
+  int bodyDoF = 0;
+  for (int b = 0; b < me->nbodies; b++) bodyDoF += me->body[b].dof;
+  *RotDoF = bodyDoF - 3 * me->nbodies;
+  *DoF = 3 * me->nfree + bodyDoF - 3;
   check_actual_interactions(me);
   int need = 0;
   for (int l = 0; l < me->nlayers; l++) need |= me->coul[l].requires_kspace;
@@ -1554,24 +1654,50 @@ void EmDee_upload(tEmDee* md, char* option, double* address) {
   } else if (!strcmp(item, "coordinates")) {
     if (!me->R) me->R = (double*)xmalloc(sizeof(double) * n3);
     memcpy(me->R, address, sizeof(double) * n3);
-    if (me->initialized) mark_stale(me, md);
-    else if (me->Lbox) initialize_system(md);
+    if (me->initialized) {
+      mark_stale(me, md);
+      if (md->Options.AutoBodyUpdate) update_rigid_bodies(me);
+    } else if (me->Lbox) {
+      initialize_system(md);
+    }
   } else if (!strcmp(item, "momenta")) {
     if (!me->initialized) error("upload", "box and coordinates have not been defined");
-    double t2[3] = {0, 0, 0};
-    for (int i = 0; i < me->natoms; i++)
+    double t2[3] = {0, 0, 0}, r2[3] = {0, 0, 0};   /* src/EmDeeData.f90:157-189 */
+    for (int j = 0; j < me->nfree; j++) {
+      int i = me->freeAtom[j] - 1;
       for (int d = 0; d < 3; d++) {
         me->P[3 * i + d] = address[3 * i + d];
-        t2[d] += me->invMass[i] * address[3 * i + d] * address[3 * i + d];
+        t2[d] += me->invMass[i] * (address[3 * i + d] * address[3 * i + d]);
       }
-    for (int d = 0; d < 3; d++) {
-      md->Kinetic.TransPart[d] = 0.5 * t2[d];
-      md->Kinetic.RotPart[d] = 0.0;
     }
-    md->Kinetic.Rotational = 0.0;
-    md->Kinetic.Total = md->Kinetic.TransPart[0] + md->Kinetic.TransPart[1] + md->Kinetic.TransPart[2];
+    for (int b = 0; b < me->nbodies; b++) {
+      obody* B = &me->body[b];
+      double Lm[3] = {0, 0, 0}, v[3], pi[4];
+      for (int d = 0; d < 3; d++) B->pcm[d] = 0.0;
+      for (int k = 0; k < B->NP; k++) {
+        const double* Pj = &address[3 * (B->index[k] - 1)];
+        double c[3];
+        for (int d = 0; d < 3; d++) B->pcm[d] += Pj[d];
+        cross3(&B->delta[3 * k], Pj, c);
+        for (int d = 0; d < 3; d++) Lm[d] += c[d];
+      }
+      for (int d = 0; d < 3; d++) {
+        t2[d] += B->invMass * (B->pcm[d] * B->pcm[d]);
+        v[d] = 2.0 * Lm[d];
+      }
+      matC(B->q, v, pi);
+      body_assign_pi(B, pi);
+      for (int d = 0; d < 3; d++) r2[d] += B->MoI[d] * (B->omega[d] * B->omega[d]);
+    }
+    for (int d = 0; d < 3; d++) {
+      md->Kinetic.RotPart[d] = 0.5 * r2[d];
+      md->Kinetic.TransPart[d] = 0.5 * t2[d];
+    }
+    md->Kinetic.Rotational = md->Kinetic.RotPart[0] + md->Kinetic.RotPart[1] + md->Kinetic.RotPart[2];
+    md->Kinetic.Total = md->Kinetic.TransPart[0] + md->Kinetic.TransPart[1] + md->Kinetic.TransPart[2] +
+                        md->Kinetic.Rotational;
     md->Kinetic.ShadowKinetic = md->Kinetic.Total;
-    md->Kinetic.ShadowRotational = 0.0;
+    md->Kinetic.ShadowRotational = md->Kinetic.Rotational;
     md->Kinetic.UpToDate = true;
   } else if (!strcmp(item, "forces")) {
     if (!me->initialized) error("upload", "box and coordinates have not been defined");
@@ -1601,12 +1727,36 @@ void EmDee_download(tEmDee md, char* option, double* address) {
     if (!me->R) error("download", "coordinates have not been allocated");
     memcpy(address, me->R, sizeof(double) * n3);
   } else if (!strcmp(item, "momenta")) {
-    memcpy(address, me->P, sizeof(double) * n3);
+    for (int j = 0; j < me->nfree; j++)
+      for (int d = 0; d < 3; d++) address[3 * (me->freeAtom[j] - 1) + d] = me->P[3 * (me->freeAtom[j] - 1) + d];
+    for (int b = 0; b < me->nbodies; b++) particle_momenta(&me->body[b], address);
   } else if (!strcmp(item, "forces")) {
     if (!me->forcesUpToDate[me->layer - 1]) EmDee_compute_forces(&md);
     memcpy(address, me->F, sizeof(double) * n3);
   } else if (!strcmp(item, "centersOfMass")) {
-    memcpy(address, me->R, sizeof(double) * n3);
+    for (int b = 0; b < me->nbodies; b++)
+      for (int d = 0; d < 3; d++) address[3 * b + d] = me->body[b].rcm[d];
+    for (int j = 0; j < me->nfree; j++)
+      for (int d = 0; d < 3; d++) address[3 * (me->nbodies + j) + d] = me->R[3 * (me->freeAtom[j] - 1) + d];
+  } else if (!strcmp(item, "quaternions") || !strcmp(item, "quatmom") || !strcmp(item, "quattau")) {
+    for (int b = 0; b < me->nbodies; b++) {
+      obody* B = &me->body[b];
+      if (!strcmp(item, "quaternions")) for (int d = 0; d < 4; d++) address[4 * b + d] = B->q[d];
+      else if (!strcmp(item, "quatmom")) for (int d = 0; d < 4; d++) address[4 * b + d] = B->pi[d];
+      else {
+        double v[3] = {2.0 * B->tau[0], 2.0 * B->tau[1], 2.0 * B->tau[2]};
+        matC(B->q, v, &address[4 * b]);
+      }
+    }
+  } else if (!strcmp(item, "angmom") || !strcmp(item, "bodycoord") || !strcmp(item, "bodymom") ||
+             !strcmp(item, "bodyforces") || !strcmp(item, "torques") || !strcmp(item, "inertia")) {
+    for (int b = 0; b < me->nbodies; b++) {
+      obody* B = &me->body[b];
+      const double* v = !strcmp(item, "angmom") ? B->omega : !strcmp(item, "bodycoord") ? B->rcm :
+                        !strcmp(item, "bodymom") ? B->pcm : !strcmp(item, "bodyforces") ? B->F :
+                        !strcmp(item, "torques") ? B->tau : B->MoI;
+      for (int d = 0; d < 3; d++) address[3 * b + d] = v[d];
+    }
   } else {
     error("download", "invalid option");
   }
@@ -1651,10 +1801,31 @@ void EmDee_share_phase_space(tEmDee mdkeep, tEmDee* mdlose) {   /* src/EmDeeCode
 /* dynamics (src/EmDeeCode.f90:950-1103, src/EmDeeData.f90:823-922)           */
 /* ======================================================================== */
 
+/* src/EmDeeCode.f90:950-1020 */
 void EmDee_random_momenta(tEmDee* md, double kT, bool adjust, int seed) {
   odata* me = get(*md);
-  double twoKEt[3] = {0, 0, 0};
+  double twoKEt[3] = {0, 0, 0}, twoKEr[3] = {0, 0, 0};
   if (me->random.seeding_required) rng_setup(&me->random, seed);
+  if (me->nbodies != 0) {
+    if (!me->initialized) error("random_momenta", "coordinates have not defined");
+    for (int b = 0; b < me->nbodies; b++) {
+      obody* B = &me->body[b];
+      double f = sqrt(B->mass * kT), w[3];
+      double a0 = rng_normal(&me->random), a1 = rng_normal(&me->random), a2 = rng_normal(&me->random);
+      B->pcm[0] = f * a0;
+      B->pcm[1] = f * a1;
+      B->pcm[2] = f * a2;
+      double c0 = rng_normal(&me->random), c1 = rng_normal(&me->random), c2 = rng_normal(&me->random);
+      w[0] = sqrt(B->invMoI[0] * kT) * c0;
+      w[1] = sqrt(B->invMoI[1] * kT) * c1;
+      w[2] = sqrt(B->invMoI[2] * kT) * c2;
+      body_assign_omega(B, w);
+      for (int d = 0; d < 3; d++) {
+        twoKEt[d] += B->invMass * (B->pcm[d] * B->pcm[d]);
+        twoKEr[d] += B->MoI[d] * (B->omega[d] * B->omega[d]);
+      }
+    }
+  }
   for (int j = 0; j < me->nfree; j++) {
     int i = me->freeAtom[j] - 1;
     double s = sqrt(me->mass[i] * kT);
@@ -1666,10 +1837,13 @@ void EmDee_random_momenta(tEmDee* md, double kT, bool adjust, int seed) {
   }
   if (adjust) {   /* src/EmDeeCode.f90:994-1018 */
     double vcm[3];
+    int bodyDoF = 0;
+    for (int b = 0; b < me->nbodies; b++) bodyDoF += me->body[b].dof;
     for (int d = 0; d < 3; d++) {
-      double s = 0.0;
+      double s = 0.0, sb = 0.0;
       for (int j = 0; j < me->nfree; j++) s += me->P[3 * (me->freeAtom[j] - 1) + d];
-      vcm[d] = (s + 0.0) / me->totalMass;
+      for (int b = 0; b < me->nbodies; b++) sb += me->body[b].pcm[d];
+      vcm[d] = (s + sb) / me->totalMass;
       twoKEt[d] = 0.0;
     }
     for (int j = 0; j < me->nfree; j++) {
@@ -1679,59 +1853,105 @@ void EmDee_random_momenta(tEmDee* md, double kT, bool adjust, int seed) {
         twoKEt[d] += me->invMass[i] * (me->P[3 * i + d] * me->P[3 * i + d]);
       }
     }
-    double sum = (twoKEt[0] + 0.0) + (twoKEt[1] + 0.0) + (twoKEt[2] + 0.0);
-    double factor = sqrt((double)(3 * me->nfree + 0 - 3) * kT / sum);
+    for (int b = 0; b < me->nbodies; b++) {
+      obody* B = &me->body[b];
+      for (int d = 0; d < 3; d++) {
+        B->pcm[d] = B->pcm[d] - B->mass * vcm[d];
+        twoKEt[d] += B->invMass * (B->pcm[d] * B->pcm[d]);
+      }
+    }
+    double sum = (twoKEt[0] + twoKEr[0]) + (twoKEt[1] + twoKEr[1]) + (twoKEt[2] + twoKEr[2]);
+    double factor = sqrt((double)(3 * me->nfree + bodyDoF - 3) * kT / sum);
     for (int j = 0; j < me->nfree; j++)
       for (int d = 0; d < 3; d++) me->P[3 * (me->freeAtom[j] - 1) + d] *= factor;
-    for (int d = 0; d < 3; d++) twoKEt[d] = factor * factor * twoKEt[d];
+    for (int b = 0; b < me->nbodies; b++) {
+      obody* B = &me->body[b];
+      double w[3] = {factor * B->omega[0], factor * B->omega[1], factor * B->omega[2]};
+      for (int d = 0; d < 3; d++) B->pcm[d] = factor * B->pcm[d];
+      body_assign_omega(B, w);
+    }
+    for (int d = 0; d < 3; d++) {
+      twoKEt[d] = factor * factor * twoKEt[d];
+      twoKEr[d] = factor * factor * twoKEr[d];
+    }
   }
   for (int d = 0; d < 3; d++) {
-    md->Kinetic.RotPart[d] = 0.0;
+    md->Kinetic.RotPart[d] = 0.5 * twoKEr[d];
     md->Kinetic.TransPart[d] = 0.5 * twoKEt[d];
   }
-  md->Kinetic.Rotational = 0.0;
-  md->Kinetic.Total = md->Kinetic.TransPart[0] + md->Kinetic.TransPart[1] + md->Kinetic.TransPart[2] + 0.0;
+  md->Kinetic.Rotational = md->Kinetic.RotPart[0] + md->Kinetic.RotPart[1] + md->Kinetic.RotPart[2];
+  md->Kinetic.Total = md->Kinetic.TransPart[0] + md->Kinetic.TransPart[1] + md->Kinetic.TransPart[2] +
+                      md->Kinetic.Rotational;
   md->Kinetic.ShadowKinetic = md->Kinetic.Total;
-  md->Kinetic.ShadowRotational = 0.0;
+  md->Kinetic.ShadowRotational = md->Kinetic.Rotational;
   md->Kinetic.UpToDate = true;
 }
 
-void EmDee_boost(tEmDee* md, double lambda, double alpha, double dt) {   /* src/EmDeeCode.f90:1024-1065 */
+/* src/EmDeeCode.f90:1024-1065 with src/EmDeeData.f90:864-922 */
+void EmDee_boost(tEmDee* md, double lambda, double alpha, double dt) {
   odata* me = get(*md);
   double CF = phi(alpha * dt) * dt, CP = 1.0 - alpha * CF;
   int nt = me->nthreads, compute = md->Options.Compute;
+  int translate = md->Options.Translate, rotate = md->Options.Rotate;
   CF = lambda * CF;
   if (lambda != 0.0 && !me->forcesUpToDate[me->layer - 1]) EmDee_compute_forces(md);
-  double* t2 = (double*)xcalloc((size_t)3 * nt, sizeof(double));
+  double* t2 = (double*)xcalloc((size_t)6 * nt, sizeof(double));
   const double* F = me->F;
 #pragma omp parallel num_threads(nt)
   {
     int thread = omp_get_thread_num() + 1;
     int a1 = (thread - 1) * me->threadFreeAtoms + 1;
     int aN = thread * me->threadFreeAtoms < me->nfree ? thread * me->threadFreeAtoms : me->nfree;
-    if (md->Options.Translate)
-      for (int q = a1; q <= aN; q++) {   /* src/EmDeeData.f90:864-896 */
+    int b1 = (thread - 1) * me->threadBodies;
+    int bN = thread * me->threadBodies < me->nbodies ? thread * me->threadBodies : me->nbodies;
+    for (int b = b1; b < bN; b++) force_and_torque(&me->body[b], F);
+    if (translate) {
+      for (int b = b1; b < bN; b++)
+        for (int d = 0; d < 3; d++) me->body[b].pcm[d] = CP * me->body[b].pcm[d] + CF * me->body[b].F[d];
+      for (int q = a1; q <= aN; q++) {
         int j = me->freeAtom[q - 1] - 1;
         for (int d = 0; d < 3; d++) me->P[3 * j + d] = CP * me->P[3 * j + d] + CF * F[3 * j + d];
       }
-    if (compute && md->Options.Translate) {   /* src/EmDeeData.f90:900-922 */
-      double* tk = &t2[3 * (thread - 1)];
-      for (int q = a1; q <= aN; q++) {
-        int j = me->freeAtom[q - 1] - 1;
-        for (int d = 0; d < 3; d++) tk[d] += me->invMass[j] * (me->P[3 * j + d] * me->P[3 * j + d]);
+    }
+    if (rotate) {
+      double Ctau = 2.0 * CF;
+      for (int b = b1; b < bN; b++) {
+        obody* B = &me->body[b];
+        double v[3] = {Ctau * B->tau[0], Ctau * B->tau[1], Ctau * B->tau[2]}, c[4], pi[4];
+        matC(B->q, v, c);
+        for (int k = 0; k < 4; k++) pi[k] = CP * B->pi[k] + c[k];
+        body_assign_pi(B, pi);
       }
+    }
+    if (compute) {   /* src/EmDeeData.f90:900-922 */
+      double* tk = &t2[6 * (thread - 1)];
+      if (translate) {
+        for (int b = b1; b < bN; b++)
+          for (int d = 0; d < 3; d++) tk[d] += me->body[b].invMass * (me->body[b].pcm[d] * me->body[b].pcm[d]);
+        for (int q = a1; q <= aN; q++) {
+          int j = me->freeAtom[q - 1] - 1;
+          for (int d = 0; d < 3; d++) tk[d] += me->invMass[j] * (me->P[3 * j + d] * me->P[3 * j + d]);
+        }
+      }
+      if (rotate)
+        for (int b = b1; b < bN; b++)
+          for (int d = 0; d < 3; d++) tk[3 + d] += me->body[b].MoI[d] * (me->body[b].omega[d] * me->body[b].omega[d]);
     }
   }
   if (compute) {
-    if (md->Options.Translate)
+    if (translate)
       for (int d = 0; d < 3; d++) {
         double s = t2[d];
-        for (int t = 1; t < nt; t++) s += t2[3 * t + d];
+        for (int t = 1; t < nt; t++) s += t2[6 * t + d];
         md->Kinetic.TransPart[d] = 0.5 * s;
       }
-    if (md->Options.Rotate) {
-      for (int d = 0; d < 3; d++) md->Kinetic.RotPart[d] = 0.0;
-      md->Kinetic.Rotational = 0.0;
+    if (rotate) {
+      for (int d = 0; d < 3; d++) {
+        double s = t2[3 + d];
+        for (int t = 1; t < nt; t++) s += t2[6 * t + 3 + d];
+        md->Kinetic.RotPart[d] = 0.5 * s;
+      }
+      md->Kinetic.Rotational = md->Kinetic.RotPart[0] + md->Kinetic.RotPart[1] + md->Kinetic.RotPart[2];
     }
     md->Kinetic.Total = md->Kinetic.TransPart[0] + md->Kinetic.TransPart[1] + md->Kinetic.TransPart[2] +
                         md->Kinetic.Rotational;
@@ -1740,9 +1960,11 @@ void EmDee_boost(tEmDee* md, double lambda, double alpha, double dt) {   /* src/
   free(t2);
 }
 
-void EmDee_displace(tEmDee* md, double lambda, double alpha, double dt) {   /* src/EmDeeCode.f90:1069-1103 */
+/* src/EmDeeCode.f90:1069-1103 with src/EmDeeData.f90:823-860 */
+void EmDee_displace(tEmDee* md, double lambda, double alpha, double dt) {
   odata* me = get(*md);
   double CR, CP;
+  int translate = md->Options.Translate, rotate = md->Options.Rotate, mode = md->Options.RotationMode;
   md->Time.Motion -= omp_get_wtime();
   if (alpha != 0.0) {
     CP = phi(alpha * dt) * dt;
@@ -1753,17 +1975,31 @@ void EmDee_displace(tEmDee* md, double lambda, double alpha, double dt) {   /* s
     CR = 1.0;
   }
   CP = lambda * CP;
-  if (md->Options.Translate) {
 #pragma omp parallel num_threads(me->nthreads)
-    {
-      int thread = omp_get_thread_num() + 1;
-      int a1 = (thread - 1) * me->threadFreeAtoms + 1;
-      int aN = thread * me->threadFreeAtoms < me->nfree ? thread * me->threadFreeAtoms : me->nfree;
-      for (int q = a1; q <= aN; q++) {   /* src/EmDeeData.f90:842-846 */
+  {
+    int thread = omp_get_thread_num() + 1;
+    int a1 = (thread - 1) * me->threadFreeAtoms + 1;
+    int aN = thread * me->threadFreeAtoms < me->nfree ? thread * me->threadFreeAtoms : me->nfree;
+    int b1 = (thread - 1) * me->threadBodies;
+    int bN = thread * me->threadBodies < me->nbodies ? thread * me->threadBodies : me->nbodies;
+    if (translate) {
+      for (int b = b1; b < bN; b++) {
+        obody* B = &me->body[b];
+        for (int d = 0; d < 3; d++) B->rcm[d] = CR * B->rcm[d] + CP * B->invMass * B->pcm[d];
+      }
+      for (int q = a1; q <= aN; q++) {
         int j = me->freeAtom[q - 1] - 1;
         for (int d = 0; d < 3; d++) me->R[3 * j + d] = CR * me->R[3 * j + d] + CP * me->P[3 * j + d] * me->invMass[j];
       }
     }
+    if (rotate)
+      for (int b = b1; b < bN; b++) {
+        obody* B = &me->body[b];
+        if (mode == 0) rotate_exact(B, dt);
+        else rotate_no_squish(B, dt, mode);
+        for (int k = 0; k < B->NP; k++)
+          for (int d = 0; d < 3; d++) me->R[3 * (B->index[k] - 1) + d] = B->rcm[d] + B->delta[3 * k + d];
+      }
   }
   mark_stale(me, md);
   md->Time.Motion += omp_get_wtime();

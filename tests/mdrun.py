@@ -86,13 +86,20 @@ COUL_MODELS = {
 }
 
 
-def setup_water(lib, cfg, coul, pair="shifted_force", precision=None, natoms=None, exclusions=True):
-    """SPC/E sample as free atoms (test/test_coul_*.f90:33-48 without rigid bodies):
-    O-O Lennard-Jones (H: pair_none), the Coulomb model `coul`, intramolecular
-    pairs excluded with EmDee_ignore_pair."""
+def setup_water(lib, cfg, coul, pair="shifted_force", precision=None, natoms=None, exclusions=True,
+                rigid=False, coords_first=False):
+    """SPC/E sample (test/test_coul_*.f90:33-48): O-O Lennard-Jones (H:
+    pair_none) and the Coulomb model `coul`.  With rigid=False the molecules are
+    free atoms whose intramolecular pairs are excluded with EmDee_ignore_pair;
+    with rigid=True each molecule is a rigid body (EmDee_system's `bodies`
+    argument, test/test_rigid_body_exact.f90:35), which drops its internal pairs
+    from the neighbor lists.  coords_first uploads the coordinates before the box
+    (test/test_rigid_body_exact.f90:46-48), so the bodies are set up when the box
+    arrives."""
     run = cfg["run"]
     N = natoms or len(cfg["coordinates"])
-    md = lib.system(1, 1, run["Rc"], run["skin"], N, cfg["type"][:N], cfg["mass"])
+    bodies = cfg["molecule"][:N] if rigid else None
+    md = lib.system(1, 1, run["Rc"], run["skin"], N, cfg["type"][:N], cfg["mass"], bodies)
     if precision is not None:
         lib.EmDee_set_precision(md, precision)
     for i, (eps, sig) in enumerate(zip(cfg["epsilon"], cfg["sigma"])):
@@ -104,7 +111,7 @@ def setup_water(lib, cfg, coul, pair="shifted_force", precision=None, natoms=Non
             p = lib.EmDee_shifted_force(lib.EmDee_pair_lj_cut(eps / run["mvv2e"], sig))
         lib.EmDee_set_pair_model(md, i + 1, i + 1, p, run["kCoul"])
     lib.EmDee_set_coul_model(md, COUL_MODELS[coul](lib))
-    if exclusions:
+    if exclusions and not rigid:
         mol = cfg["molecule"][:N]
         first = {}
         for a, m in enumerate(mol):
@@ -114,6 +121,10 @@ def setup_water(lib, cfg, coul, pair="shifted_force", precision=None, natoms=Non
                 for y in range(x + 1, len(atoms)):
                     lib.EmDee_ignore_pair(md, atoms[x], atoms[y])
     lib.upload(md, "charges", cfg["charge"][:N])
-    lib.upload(md, "box", np.array([cfg["box"]]))
-    lib.upload(md, "coordinates", np.array(cfg["coordinates"][:N]))
+    if coords_first:
+        lib.upload(md, "coordinates", np.array(cfg["coordinates"][:N]))
+        lib.upload(md, "box", np.array([cfg["box"]]))
+    else:
+        lib.upload(md, "box", np.array([cfg["box"]]))
+        lib.upload(md, "coordinates", np.array(cfg["coordinates"][:N]))
     return md
