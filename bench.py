@@ -287,6 +287,15 @@ def run_gpu(args):
                     "unit": "GB/s", "frac": (move_gbs / hbm) if move_gbs else None, "traffic": None,
                     "peak_source": peak_kind, "boost_achieved_gbs": boost_gbs}
 
+    # whole step against both ceilings: max(FLOPs / FP32 peak, bytes / HBM peak) per step
+    # (pair FLOPs as above; 152 B per atom-step of integrator and force I/O)
+    step_flops, step_bytes = flops, 152.0 * N
+    step_s = ms / args.steps * 1e-3
+    step_floor = max(step_flops / (fp32_peak * 1e12), step_bytes / (hbm * 1e9))
+    roofline_step = {"bound": "fp32" if step_flops / (fp32_peak * 1e12) >= step_bytes / (hbm * 1e9) else "hbm",
+                     "floor_us": step_floor * 1e6, "measured_us": step_s * 1e6, "frac": step_floor / step_s,
+                     "flops_per_step": step_flops, "bytes_per_step": step_bytes}
+
     # ---- end to end through the C ABI with host buffers ----
     pin = lambda: torch.empty((N, 3), dtype=torch.float64, pin_memory=True).numpy()
     Ph, Rh = pin(), pin()
@@ -332,6 +341,7 @@ def run_gpu(args):
                            "l2": "no flush; per-step working set (R, P, F, packed positions, lists) ~0.4 GB "
                                  "> 129 MB L2"},
                 "clocks": clk, "gpu_launches": int(launches), "roofline": roofline, "roofline_hbm": roofline_hbm,
+                "roofline_step": roofline_step,
                 "kernels": per_kernel, "e2e": e2e, "cpu_baseline": cpu}
         print(json.dumps(line))
     if world > 1:
