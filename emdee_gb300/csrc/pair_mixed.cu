@@ -12,6 +12,7 @@
 // Per-thread energy and virial sums are promoted to FP64 for the block and grid
 // reductions.
 #include <algorithm>
+#include <cstdlib>
 
 #include "reduce.cuh"
 #include "system.hpp"
@@ -106,27 +107,35 @@ __global__ void __launch_bounds__(PAIR_THREADS) k_pair_mixed(PairArgsF A) {
           dz -= A.Mf * rintf(dz / A.Mf);
         }
         const float r2 = dx * dx + dy * dy + dz * dz;
-        if (r2 < A.rc2) {
+        if (VAR == 0) {
+          // branch-free: every entry runs the same code; entries beyond the
+          // cut-off (and sentinels) are zeroed by selects, so the 8 entries of
+          // a chunk form one straight-line block the compiler can interleave
+          constexpr bool needR = MOD == SHIFTED_FORCE || MOD == SMOOTHED || MOD == SHIFTED_SMOOTHED;
+          const bool in = r2 < A.rc2;
+          const float invR2c = Ops<float>::rcp(r2);
+          const float invR2 = invR2c * A.invw2;
+          const float invR = needR ? sqrtf(invR2) : 1.f;
+          const float sr2 = m0.sigsq * invR2, sr6 = sr2 * sr2 * sr2, sr12 = sr6 * sr6;
+          float E = m0.eps4 * (sr12 - sr6), W = m0.eps24 * (sr12 + sr12 - sr6);
+          if (MOD != NONE) modifier_compute(m0, E, W, invR, invR2);
+          W = in ? W : 0.f;
+          if (COUNT) within += in ? 1.f : 0.f;
+          if (COMPUTE) Ep += in ? E : 0.f;
+          Wp += W;
+          const float s = W * invR2c;
+          fx += s * dx;
+          fy += s * dy;
+          fz += s * dz;
+        } else if (r2 < A.rc2) {
           if (COUNT) within += 1.f;
           const float invR2c = Ops<float>::rcp(r2);
           const float invR2 = invR2c * A.invw2;
-          float Wsum;
-          if (VAR == 0) {
-            constexpr bool needR = MOD == SHIFTED_FORCE || MOD == SMOOTHED || MOD == SHIFTED_SMOOTHED;
-            const float invR = needR ? sqrtf(invR2) : 1.f;
-            float sr2 = m0.sigsq * invR2, sr6 = sr2 * sr2 * sr2, sr12 = sr6 * sr6;
-            float E = m0.eps4 * (sr12 - sr6), W = m0.eps24 * (sr12 + sr12 - sr6);
-            if (MOD != NONE) modifier_compute(m0, E, W, invR, invR2);
-            if (COMPUTE) Ep += E;
-            Wp += W;
-            Wsum = W;
-          } else {
-            const int tj = htype[qj];
-            const PairEntry<float>& pe = tbl[ti * A.ntypes + tj];
-            const float invR = sqrtf(invR2);
-            const bool ijch = pi.w != 0.f && pj.w != 0.f;
-            Wsum = pair_eval<float, COMPUTE>(pe, coul, ijch, pi.w, pj.w, invR, invR2, Ep, Ec, Wp, Wc);
-          }
+          const int tj = htype[qj];
+          const PairEntry<float>& pe = tbl[ti * A.ntypes + tj];
+          const float invR = sqrtf(invR2);
+          const bool ijch = pi.w != 0.f && pj.w != 0.f;
+          const float Wsum = pair_eval<float, COMPUTE>(pe, coul, ijch, pi.w, pj.w, invR, invR2, Ep, Ec, Wp, Wc);
           const float s = Wsum * invR2c;
           fx += s * dx;
           fy += s * dy;
@@ -144,7 +153,7 @@ __global__ void __launch_bounds__(PAIR_THREADS) k_pair_mixed(PairArgsF A) {
   }
   // each pair is visited from both atoms: halve the sums
   const float v[5] = {0.5f * Ep, 0.5f * Ec, 0.5f * Wp, 0.5f * Wc, 0.5f * within};
-  grid_reduce_f32<5, PAIR_THREADS>(v, A.partials, A.ticket, A.result);
+  grid_reduce_ff<5, PAIR_THREADS>(v, reinterpret_cast<float2*>(A.partials), A.ticket, A.result);
 }
 
 template <bool COMPUTE, int VAR, int MOD, bool MINIMG, bool COUNT>
@@ -202,7 +211,11 @@ void device_pair_forces_mixed(System& s, bool compute, bool useInRc, double rc2s
   size_t smem = (size_t)(g.maxHalo + 1) * sizeof(float4) + sizeof(int) * (3 * g.haloCells + 1);
   if (variant != 0) smem += sizeof(PairEntry<float>) * s.ntypes * s.ntypes + g.maxHalo + 17;
   const bool mi = g.M == 5;
-  const int th = std::min(PAIR_THREADS, std::max(32, g.tileStride));
+  // threads per block: one per tile atom up to the tile's largest count, or
+  // fewer with several atoms per thread (EMDEE_PAIR_THREADS, a multiple of 32)
+  static const int thEnv = getenv("EMDEE_PAIR_THREADS") ? atoi(getenv("EMDEE_PAIR_THREADS")) : 0;
+  const int th = thEnv >= 32 && thEnv % 32 == 0 ? std::min(thEnv, PAIR_THREADS)
+                                                 : std::min(PAIR_THREADS, std::max(32, g.tileStride));
   const int nt = g.nTiles;
   if (variant == 0) {
     const int mod = s.P(0, 0, s.layer - 1).model.p.modifier;

@@ -105,4 +105,85 @@ __device__ __forceinline__ void grid_reduce_f32(const float (&v)[NQ], double* pa
   grid_reduce_lane0<NQ, THREADS>(w, partials, ticket, result);
 }
 
+// ---- float-float (FP32 pair) reductions: every level on the FP32 pipe ----------
+//
+// A value is carried as hi + lo with |lo| << |hi|; additions use Knuth's
+// error-free two-sum on the high parts and plain addition of the low parts, so
+// the sum keeps about 48 significant bits.  Only the final hi + lo conversion
+// per quantity touches FP64.
+
+__device__ __forceinline__ void ff_add(float& hi, float& lo, float bh, float bl) {
+  const float s = hi + bh, bp = s - hi, err = (hi - (s - bp)) + (bh - bp);
+  hi = s;
+  lo = lo + bl + err;
+}
+
+template <int NQ>
+__device__ __forceinline__ void warp_sum_ff(float (&hi)[NQ], float (&lo)[NQ]) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int q = 0; q < NQ; q++) {
+      const float h2 = __shfl_down_sync(0xffffffffu, hi[q], o), l2 = __shfl_down_sync(0xffffffffu, lo[q], o);
+      ff_add(hi[q], lo[q], h2, l2);
+    }
+}
+
+// Per-thread FP32 values -> result[q] (FP64).  partials holds NQ float2 per block.
+// The last block (ticket) sums the partials in block order; the result does not
+// depend on block scheduling.
+template <int NQ, int THREADS>
+__device__ __forceinline__ void grid_reduce_ff(const float (&v)[NQ], float2* partials, unsigned int* ticket,
+                                               double* result) {
+  __shared__ float2 red[NQ][THREADS / 32];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  float hi[NQ], lo[NQ];
+#pragma unroll
+  for (int q = 0; q < NQ; q++) {
+    hi[q] = v[q];
+    lo[q] = 0.f;
+  }
+  warp_sum_ff<NQ>(hi, lo);
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < NQ; q++) red[q][warp] = make_float2(hi[q], lo[q]);
+  __syncthreads();
+  if (threadIdx.x < NQ) {
+    const int q = threadIdx.x;
+    float h = 0.f, l = 0.f;
+    for (int w = 0; w < nw; w++) ff_add(h, l, red[q][w].x, red[q][w].y);
+    partials[(size_t)blockIdx.x * NQ + q] = make_float2(h, l);
+    __threadfence();   // the partial is visible before the ticket counts this block
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+#pragma unroll
+  for (int q = 0; q < NQ; q++) {
+    hi[q] = 0.f;
+    lo[q] = 0.f;
+  }
+  for (unsigned int b = threadIdx.x; b < gridDim.x; b += blockDim.x)
+#pragma unroll
+    for (int q = 0; q < NQ; q++) {
+      const float2 x = __ldcg(&partials[(size_t)b * NQ + q]);
+      ff_add(hi[q], lo[q], x.x, x.y);
+    }
+  warp_sum_ff<NQ>(hi, lo);
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < NQ; q++) red[q][warp] = make_float2(hi[q], lo[q]);
+  __syncthreads();
+  if (threadIdx.x < NQ) {
+    const int q = threadIdx.x;
+    float h = 0.f, l = 0.f;
+    for (int w = 0; w < nw; w++) ff_add(h, l, red[q][w].x, red[q][w].y);
+    result[q] = (double)h + (double)l;
+  }
+  if (threadIdx.x == 0) *ticket = 0;
+}
+
 }  // namespace emdee
