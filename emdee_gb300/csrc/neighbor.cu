@@ -364,7 +364,7 @@ __device__ __forceinline__ bool excluded(const BuildArgs& A, int a, int b) {
   return false;
 }
 
-static const int BUILD_THREADS = 128;
+static const int BUILD_THREADS = 256;   // upper bound; launches use one thread per tile atom
 
 // List layout: for tile t, chunk c (8 entries) and tile-local atom li, the
 // entries 8c..8c+7 of atom li are 16 contiguous bytes at
@@ -375,6 +375,8 @@ __device__ __forceinline__ size_t nb_index(int t, int capC, int tileStride, int 
   return (((size_t)t * capC + (n >> 3)) * tileStride + li) * 8 + (n & 7);
 }
 
+// GENERAL: several atom types, bodies, exclusions or layered lists; MINIMG: M = 5.
+template <bool GENERAL, bool MINIMG>
 __global__ void __launch_bounds__(BUILD_THREADS) k_build(BuildArgs A) {
   extern __shared__ __align__(16) unsigned char sraw[];
   __shared__ int ws[33];
@@ -385,15 +387,16 @@ __global__ void __launch_bounds__(BUILD_THREADS) k_build(BuildArgs A) {
   int* off = hslot + A.haloCap + 1;
   int* cst = off + g.haloCells + 1;
   int* hxyz = cst + g.haloCells;
-  const bool single = A.ntypes == 1;
+  const bool single = !GENERAL || A.ntypes == 1;
   uint8_t* sinter = (uint8_t*)(hxyz + g.haloCells);
   uint8_t* htype = sinter + A.ntypes * A.ntypes;
   for (int k = threadIdx.x; k < A.ntypes * A.ntypes; k += blockDim.x) sinter[k] = A.interact[k];
   halo_layout(g, t, A.tab, A.start, off, cst, hxyz, ws);
   stage_frame(g, off, cst, hxyz, A.pos4, hpos, hslot, single ? (uint8_t*)nullptr : htype, A.type8);
   __syncthreads();
-  const bool none = single && !sinter[0];   // the only type pair does not interact: empty lists
-  const bool filterByAtom = A.hasBodies || A.hasEx;
+  const bool none = A.ntypes == 1 && !sinter[0];   // the only type pair does not interact: empty lists
+  const bool filterByAtom = GENERAL && (A.hasBodies || A.hasEx);
+  const bool layered = GENERAL && A.layered;
   const int tb = A.start[t * cells], te = A.start[(t + 1) * cells];
   const int HW = g.HW, capC = A.cap >> 3, chunkStride = A.tileStride * 8;
   for (int li = threadIdx.x; li < te - tb; li += blockDim.x) {
@@ -404,11 +407,11 @@ __global__ void __launch_bounds__(BUILD_THREADS) k_build(BuildArgs A) {
     A.selfIdx[si] = (uint16_t)myq;
     const float4 pi = hpos[myq];
     const int ai = A.orig[si], ti = single ? 0 : A.type8[si];
-    const int bi = A.hasBodies ? A.body[ai] : -1;
-    const bool hasEx = A.hasEx && A.exCount[ai] > 0;
+    const int bi = filterByAtom && A.hasBodies ? A.body[ai] : -1;
+    const bool hasEx = filterByAtom && A.hasEx && A.exCount[ai] > 0;
     uint16_t* myList = A.nb + ((size_t)t * capC * A.tileStride + li) * 8;
     int n = 0, nIn = 0;
-    for (int pass = 0; pass <= A.layered && !none; pass++) {
+    for (int pass = 0; pass <= (layered ? 1 : 0) && !none; pass++) {
       // the 5 cells of a stencil row (dx = -2..2) are consecutive in the halo
       for (int row = 0; row < 25; row++) {
         const int h0 = (hcx - 2) + HW * ((hcy + row % 5 - 2) + HW * (hcz + row / 5 - 2));
@@ -416,7 +419,7 @@ __global__ void __launch_bounds__(BUILD_THREADS) k_build(BuildArgs A) {
         for (int q = off[h0]; q < q1; q++) {
           const float4 pj = hpos[q];
           float ex = pi.x - pj.x, ey = pi.y - pj.y, ez = pi.z - pj.z;
-          if (A.minimg) {
+          if (MINIMG) {
             ex -= A.Mf * rintf(ex / A.Mf);
             ey -= A.Mf * rintf(ey / A.Mf);
             ez -= A.Mf * rintf(ez / A.Mf);
@@ -424,13 +427,13 @@ __global__ void __launch_bounds__(BUILD_THREADS) k_build(BuildArgs A) {
           const float r2 = ex * ex + ey * ey + ez * ez;
           if (r2 >= A.hi2 || q == myq) continue;
           if (!(r2 < A.lo2 || exact_inside(A.R, A.L, ai, A.orig[hslot[q]], A.thr))) continue;
-          if (!single && !sinter[ti * A.ntypes + htype[q]]) continue;
+          if (GENERAL && !single && !sinter[ti * A.ntypes + htype[q]]) continue;
           if (filterByAtom) {
             const int aj = A.orig[hslot[q]];
             if (A.hasBodies && A.body[aj] == bi) continue;
             if (hasEx && excluded(A, ai, aj)) continue;
           }
-          if (A.layered) {
+          if (layered) {
             bool inner = r2 < A.loIn2 || (r2 < A.hiIn2 && exact_inside(A.R, A.L, ai, A.orig[hslot[q]], A.thrIn));
             if (inner == (pass == 1)) continue;
           }
@@ -611,14 +614,17 @@ void device_build_lists(System& s) {
     s.prof.total++;
   }
   size_t smem = build_smem(g, s.ntypes);
-  CK(cudaFuncSetAttribute(k_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const bool general = s.ntypes > 1 || A.hasBodies || A.hasEx || A.layered;
+  auto kb = general ? (A.minimg ? k_build<true, true> : k_build<true, false>)
+                    : (A.minimg ? k_build<false, true> : k_build<false, false>);
+  CK(cudaFuncSetAttribute(kb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   for (int attempt = 0; attempt < 3; attempt++) {
     size_t need = (size_t)g.nTiles * g.cap * g.tileStride;
     grow(g.dNb, c.nb, need);
     A.nb = g.dNb;
     A.cap = g.cap;
     CK(cudaMemsetAsync(A.maxCount, 0, sizeof(int), s.stream));
-    k_build<<<g.nTiles, BUILD_THREADS, smem, s.stream>>>(A);
+    kb<<<g.nTiles, std::min(BUILD_THREADS, std::max(32, g.tileStride)), smem, s.stream>>>(A);
     s.prof.total++;
     CK(cudaGetLastError());
     int mc = 0;
