@@ -30,6 +30,7 @@ UNITS = {
     "motion.cu": ["-fmad=false"],
     "pair_mixed.cu": [],
     "bodies.cu": ["-fmad=false"],
+    "ewald.cu": ["-fmad=false"],
 }
 HEADERS = ["system.hpp", "pairmath.cuh", "tile.cuh", "reduce.cuh", "rigid.cuh", os.path.join("..", "..", "include", "emdee.h")]
 

@@ -255,7 +255,19 @@ static void initialize_system(tEmDee* md) {   // src/EmDeeCode.f90:916-923 and s
     if (s.kspace_active) s.kspace_active = false;
     else fatal("system initialization", "a kspace solver is required, but has not been defined");
   }
-  if (s.kspace_active) fatal("system initialization", "k-space electrostatics are not available in this build");
+  if (s.kspace_active) {   // src/EmDeeData.f90:384-412
+    double kspaceRc = 0.0;
+    bool found = false;
+    for (int l = 0; l < s.nlayers; l++)
+      if (s.coul[l].requires_kspace) {
+        const double lrc = s.useInRc[l] ? s.InRc : s.Rc;
+        if (!found) kspaceRc = lrc;
+        else if (lrc != kspaceRc)
+          fatal("system initialization", "all layers with ewald-like coulomb models must have the same cutoff");
+        found = true;
+      }
+    ewald_initialize(s, kspaceRc);
+  }
   s.initialized = true;
   upload_models(s);
   upload_exclusions(s);
@@ -283,7 +295,12 @@ static void compute_forces_impl(tEmDee* md) {
   device_pack(s);
   device_pair_forces(s, compute);
   const double* r = s.hResult;   // Epair, Ecoul, Wpair, Wcoul
-  md->Virial.Total = r[2] + r[3] + 0.0 + 0.0 + 0.0;
+  double Elong = 0.0, Wlong = 0.0;
+  if (s.coul[s.layer - 1].requires_kspace) {   // src/EmDeeCode.f90:1249-1252
+    Elong = ewald_compute(s);
+    Wlong = r[1] + Elong - r[3];
+  }
+  md->Virial.Total = r[2] + r[3] + Wlong + 0.0 + 0.0;
   md->Virial.Body = 0.0;
   if (s.nbodies != 0) {   // src/EmDeeData.f90:926-953
     md->Virial.Body = bodies_virial(s);
@@ -291,10 +308,10 @@ static void compute_forces_impl(tEmDee* md) {
   }
   if (compute) {
     md->Energy.Dispersion = r[0];
-    md->Energy.Coulomb = r[1] + 0.0;
+    md->Energy.Coulomb = r[1] + Elong;
     md->Energy.Bond = 0.0;
     md->Energy.Angle = 0.0;
-    md->Energy.Potential = r[0] + r[1] + 0.0 + 0.0 + 0.0;
+    md->Energy.Potential = r[0] + r[1] + Elong + 0.0 + 0.0;
     md->Energy.ShadowPotential = md->Energy.Potential;
   }
   md->Energy.UpToDate = compute;
@@ -487,8 +504,8 @@ tEmDee EmDee_system(int threads, int layers, double rc, double skin, int N, int*
   }
   CK(cudaMallocHost(&s->hResult, sizeof(double) * 24));
   CK(cudaMalloc(&s->dResult, sizeof(double) * 24));
-  CK(cudaMalloc(&s->dTicket, sizeof(unsigned int) * 4));
-  CK(cudaMemset(s->dTicket, 0, sizeof(unsigned int) * 4));
+  CK(cudaMalloc(&s->dTicket, sizeof(unsigned int) * 8));
+  CK(cudaMemset(s->dTicket, 0, sizeof(unsigned int) * 8));
   memset(s->hResult, 0, sizeof(double) * 24);
 
   md.Builds = 0;
@@ -532,6 +549,7 @@ void EmDee_destroy(tEmDee* md) {
   cudaFree(s->dBodyD);
   cudaFree(s->dFree);
   cudaFree(s->dBodyScratch);
+  ewald_free(*s);
   cudaFree(s->dExFirst);
   cudaFree(s->dExCount);
   cudaFree(s->dExItem);

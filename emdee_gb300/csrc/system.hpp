@@ -76,6 +76,29 @@ struct GridCaps {   // allocated capacities of the grid arrays
   size_t ranks = 0, atoms = 0, tiles = 0, nb = 0, scan = 0;
 };
 
+// Ewald k-space solver (src/kspace_ewald.f90, src/modelClass_kspace.f90):
+// host set-up and device arrays.  Cubic boxes only, as the reference's Lbox.
+struct Ewald {
+  double alpha = 0, beta = 0, kmax = 0, Volume = 0, L = 0;
+  int nmax = -1, nvecs = 0, ntypes = 0, nq = 0, nTypePairs = 0;
+  std::vector<int> type;                   // charged types (1-based), ascending
+  std::vector<int> item, qtype;            // charge list: atom (0-based) and local type, type by type
+  std::vector<double> value;               // charges of the list
+  std::vector<int> first, last;            // per local type: [first, last) in the list
+  std::vector<double> Erigid;              // per type pair (symm1D order): rigid-pair and self discounts
+  std::vector<double> lambda, lambda1D;    // [layer][t][u] = kCoul(u, t); [layer][k]
+  std::vector<int> n;                      // k-vectors (nvecs x 3 integers)
+  std::vector<double> prefac, vec;         // nvecs; 3 x nvecs
+  // device
+  int *dItem = nullptr, *dQType = nullptr, *dFirst = nullptr, *dLast = nullptr;
+  double* dValue = nullptr;
+  int4* dN = nullptr;
+  double *dPrefac = nullptr, *dVec = nullptr, *dLambda = nullptr;
+  double2 *dPartial = nullptr, *dSigma = nullptr;
+  double* dEnergyPartial = nullptr;
+  size_t partialCap = 0;
+};
+
 struct Grid {
   int M = 0;            // cells per dimension (src/neighbor_lists.f90:185-186)
   int TB = 0;           // tile edge in cells
@@ -152,6 +175,7 @@ struct System {
   std::vector<Model> coul;                    // per layer
   Model kspace;
   bool kspace_active = false;
+  Ewald ewald;
   std::vector<char> multilayer, overridable, interact, pairs_exist, useInRc, bonded, forcesUpToDate;
   std::vector<tEnergy> layerEnergy;
   std::vector<tVirial> layerVirial;
@@ -229,5 +253,9 @@ void bodies_download(System& s);
 void bodies_upload(System& s);
 // Neighbor pairs (1-based, i<j) of the current lists.
 long device_neighbor_pairs(System& s, int* pairs, long capacity);
+// Ewald k-space (ewald.cu): set-up at initialization, energy + forces per call
+void ewald_initialize(System& s, double kspaceRc);
+double ewald_compute(System& s);
+void ewald_free(System& s);
 
 }  // namespace emdee

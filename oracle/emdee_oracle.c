@@ -669,7 +669,7 @@ static void cutoff_setup(omodel* m, double cutoff) {
 }
 
 /* src/modelClass_coul.f90:101-106 and src/coul_long.f90:55-64 */
-static void __attribute__((unused)) coul_kspace_setup(omodel* m, double alpha) {
+static void coul_kspace_setup(omodel* m, double alpha) {
   if (m->kind == MK_COUL_LONG) {
     m->alpha = alpha;
     m->beta = 2.0 * alpha / sqrt(3.14159265358979324);
@@ -737,6 +737,8 @@ typedef struct {
   double* value;
 } olist;
 
+#include "ewald_oracle.h"
+
 typedef struct {
   int natoms, mcells, ncells, maxcells, maxatoms, ntypes, nbodies, nfree, nthreads, threadAtoms;
   int threadFreeAtoms, nlayers, layer;
@@ -758,6 +760,7 @@ typedef struct {
   omodel* coul;        /* per layer */
   omodel kspace;
   int kspace_active;
+  oewald ewald;
   char *multilayer, *overridable, *interact, *pairs_exist;
   char *bonded, *useInRc, *forcesUpToDate;
   double* layerF;
@@ -1532,7 +1535,12 @@ void EmDee_compute_forces(tEmDee* md) {
     for (int t = 1; t < nt; t++) s += Fs[(size_t)3 * N * t + q];
     me->F[q] = s;
   }
-  if (me->coul[me->layer - 1].requires_kspace) error("compute forces", "k-space electrostatics are not handled by the oracle");
+  if (me->coul[me->layer - 1].requires_kspace) {   /* src/EmDeeCode.f90:1249-1252, src/EmDeeData.f90:689-700 */
+    ewald_prepare(&me->ewald, Rs);
+    ewald_compute(&me->ewald, me->layer, &E[2], me->F);
+    E[2] += ewald_discount_energy(&me->ewald, me->layer);
+    W[2] = E[1] + E[2] - W[1];
+  }
   md->Virial.Total = W[0] + W[1] + W[2] + W[3] + W[4];
   md->Virial.Body = 0.0;
   if (me->nbodies != 0) {   /* src/EmDeeData.f90:926-953 */
@@ -1605,6 +1613,11 @@ static void update_rigid_bodies(odata* me) {
   }
 }
 
+static double pair_kcoul(void* ctx, int itype, int jtype, int layer) {   /* me%pair%kCoul */
+  odata* me = (odata*)ctx;
+  return PAIR(me, itype - 1, jtype - 1, layer - 1).kCoul;
+}
+
 static void perform_initialization(odata* me, int* DoF, int* RotDoF) {
   update_rigid_bodies(me);
   int bodyDoF = 0;
@@ -1618,7 +1631,24 @@ static void perform_initialization(odata* me, int* DoF, int* RotDoF) {
     if (me->kspace_active) me->kspace_active = 0;
     else error("system initialization", "a kspace solver is required, but has not been defined");
   }
-  if (me->kspace_active) error("system initialization", "k-space electrostatics are not handled by the oracle");
+  if (me->kspace_active) {   /* src/EmDeeData.f90:384-412 */
+    double kspaceRc = 0.0;
+    int found = 0;
+    for (int l = 1; l <= me->nlayers; l++)
+      if (me->coul[l - 1].requires_kspace) {
+        double lrc = layer_rc(me, l);
+        if (!found) kspaceRc = lrc;
+        else if (lrc != kspaceRc)
+          error("system initialization", "all layers with ewald-like coulomb models must have the same cutoff");
+        found = 1;
+      }
+    memset(&me->ewald, 0, sizeof(me->ewald));
+    me->ewald.accuracy = me->kspace.accuracy;
+    ewald_initialize(&me->ewald, kspaceRc, *me->Lbox, me->natoms, me->atomType, me->charge, me->R, me->nbodies,
+                     me->body, me->nlayers, pair_kcoul, me);
+    for (int l = 0; l < me->nlayers; l++)
+      if (me->coul[l].requires_kspace) coul_kspace_setup(&me->coul[l], me->ewald.alpha);
+  }
   me->initialized = 1;
 }
 
