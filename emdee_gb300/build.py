@@ -31,8 +31,9 @@ UNITS = {
     "pair_mixed.cu": [],
     "bodies.cu": ["-fmad=false"],
     "ewald.cu": ["-fmad=false"],
+    "verlet.cu": ["-fmad=false"],
 }
-HEADERS = ["system.hpp", "pairmath.cuh", "tile.cuh", "reduce.cuh", "rigid.cuh", os.path.join("..", "..", "include", "emdee.h")]
+HEADERS = ["system.hpp", "pairmath.cuh", "tile.cuh", "reduce.cuh", "rigid.cuh", "bodies.cuh", os.path.join("..", "..", "include", "emdee.h")]
 
 
 def _stale(target, deps):

@@ -502,11 +502,11 @@ tEmDee EmDee_system(int threads, int layers, double rc, double skin, int N, int*
     CK(cudaMalloc(&s->dFree, sizeof(int) * (s->nfree > 0 ? s->nfree : 1)));
     if (s->nfree > 0) CK(cudaMemcpy(s->dFree, s->freeList.data(), sizeof(int) * s->nfree, cudaMemcpyHostToDevice));
   }
-  CK(cudaMallocHost(&s->hResult, sizeof(double) * 24));
-  CK(cudaMalloc(&s->dResult, sizeof(double) * 24));
+  CK(cudaMallocHost(&s->hResult, sizeof(double) * 48));
+  CK(cudaMalloc(&s->dResult, sizeof(double) * 48));
   CK(cudaMalloc(&s->dTicket, sizeof(unsigned int) * 8));
   CK(cudaMemset(s->dTicket, 0, sizeof(unsigned int) * 8));
-  memset(s->hResult, 0, sizeof(double) * 24);
+  memset(s->hResult, 0, sizeof(double) * 48);
 
   md.Builds = 0;
   md.DoF = 3 * (N - 1);
@@ -550,6 +550,11 @@ void EmDee_destroy(tEmDee* md) {
   cudaFree(s->dFree);
   cudaFree(s->dBodyScratch);
   ewald_free(*s);
+  cudaFree(s->verlet.s0);
+  cudaFree(s->verlet.r0);
+  cudaFree(s->verlet.q0);
+  cudaFree(s->verlet.partB);
+  cudaFree(s->verlet.partF);
   cudaFree(s->dExFirst);
   cudaFree(s->dExCount);
   cudaFree(s->dExItem);
@@ -1099,9 +1104,32 @@ void EmDee_compute_forces(tEmDee* md) {
   compute_forces_impl(md);
 }
 
+// src/EmDeeCode.f90:1107-1211
 void EmDee_verlet_step(tEmDee* md, double dt) {
-  (void)md; (void)dt;
-  fatal("verlet step", "not available in this build");
+  System& s = *sys_of(*md);
+  MirrorScope scope(s);
+  if (!s.initialized) fatal("verlet step", "system has not been initialized");
+  const bool compute = md->Options.Compute;
+  const int mode = md->Options.RotationMode;
+  double t0 = wtime();
+  device_verlet_pre(s, dt, compute, mode);
+  md->Time.Motion += wtime() - t0;
+  compute_forces_impl(md);   // unconditional; other layers keep their flags, as in the reference
+  double v[9];
+  device_verlet_post(s, dt, compute, mode, v);
+  if (compute) {
+    for (int d = 0; d < 3; d++) {
+      md->Kinetic.TransPart[d] = 0.5 * v[d];
+      md->Kinetic.RotPart[d] = 0.5 * v[3 + d];
+    }
+    md->Kinetic.Rotational = md->Kinetic.RotPart[0] + md->Kinetic.RotPart[1] + md->Kinetic.RotPart[2];
+    md->Kinetic.Total =
+        md->Kinetic.TransPart[0] + md->Kinetic.TransPart[1] + md->Kinetic.TransPart[2] + md->Kinetic.Rotational;
+    md->Energy.ShadowPotential = md->Energy.ShadowPotential - dt * dt * v[8] / 24.0;
+    md->Kinetic.ShadowRotational = v[7] / (6.0 * dt);
+    md->Kinetic.ShadowKinetic = (v[6] + v[7]) / (6.0 * dt);
+  }
+  md->Kinetic.UpToDate = compute;
 }
 
 void EmDee_rdf(tEmDee md, int bins, double Rc, int pairs, int itype[], int jtype[], double g[]) {

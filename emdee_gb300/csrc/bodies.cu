@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "reduce.cuh"
+#include "bodies.cuh"
 #include "rigid.cuh"
 #include "system.hpp"
 
@@ -14,14 +15,6 @@ namespace emdee {
 
 static const int BODY_THREADS = 128;
 
-struct BodyArgs {
-  BodyState* b;
-  int nb;
-  const int* atom;     // flat body-atom indices (0-based)
-  const double* M;     // flat masses
-  const double* d;     // flat body-frame coordinates
-  double* delta;       // flat space-frame offsets
-};
 
 // force_and_torque, then pcm and pi updates; 2KE translational (bodies) and
 // rotational partial sums
@@ -165,16 +158,6 @@ __global__ void __launch_bounds__(BODY_THREADS) k_move_free(double* __restrict__
 
 // ---- host side -------------------------------------------------------------------
 
-static BodyArgs body_args(System& s) {
-  BodyArgs A;
-  A.b = s.dBodies;
-  A.nb = s.nbodies;
-  A.atom = s.dBodyAtom;
-  A.M = s.dBodyM;
-  A.d = s.dBodyD;
-  A.delta = s.dBodyDelta;
-  return A;
-}
 
 static int body_blocks(int n) { return n > 0 ? (n + BODY_THREADS - 1) / BODY_THREADS : 1; }
 

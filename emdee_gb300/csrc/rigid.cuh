@@ -80,6 +80,7 @@ RB_HD void rb_assign_pi(BodyState& b, const double* pi) {
 
 // delta = C(q)^T B(q) d for the body's atoms
 RB_HD void rb_space_coords(const BodyState& b, const double* d, double* delta) {
+  if (!delta) return;   // orientation only (virtual rotations)
   for (int k = 0; k < b.NP; k++) {
     double t[4];
     rb_B(b.q, &d[3 * k], t);

@@ -99,6 +99,12 @@ struct Ewald {
   size_t partialCap = 0;
 };
 
+// scratch of EmDee_verlet_step (verlet.cu): shadow start values and reduction partials
+struct VerletScratch {
+  double *s0 = nullptr, *r0 = nullptr, *q0 = nullptr, *partB = nullptr, *partF = nullptr;
+  size_t s0Cap = 0, r0Cap = 0, q0Cap = 0, partBCap = 0, partFCap = 0;
+};
+
 struct Grid {
   int M = 0;            // cells per dimension (src/neighbor_lists.f90:185-186)
   int TB = 0;           // tile edge in cells
@@ -176,6 +182,7 @@ struct System {
   Model kspace;
   bool kspace_active = false;
   Ewald ewald;
+  VerletScratch verlet;
   std::vector<char> multilayer, overridable, interact, pairs_exist, useInRc, bonded, forcesUpToDate;
   std::vector<tEnergy> layerEnergy;
   std::vector<tVirial> layerVirial;
@@ -205,7 +212,8 @@ struct System {
   // results (pinned host copy and device): [0..3] Epair, Ecoul, Wpair, Wcoul, [4] pairs within
   // the cut-off, [6] body virial sum, [8] skin value, [9] rebuild flag, [10..12] 2KE
   // (translational) per dimension, [13..15] 2KE (rotational), [16..21] body 2KE sums
-  // (translational, rotational) of one body kernel
+  // (translational, rotational) of one body kernel, [22] k-space energy, [24..32] and
+  // [34..38] sums of the Verlet step (bodies, free atoms)
   double* hResult = nullptr;
   double* dResult = nullptr;
 
@@ -257,5 +265,8 @@ long device_neighbor_pairs(System& s, int* pairs, long capacity);
 void ewald_initialize(System& s, double kspaceRc);
 double ewald_compute(System& s);
 void ewald_free(System& s);
+// EmDee_verlet_step halves (verlet.cu)
+void device_verlet_pre(System& s, double dt, bool compute, int mode);
+void device_verlet_post(System& s, double dt, bool compute, int mode, double* out);
 
 }  // namespace emdee

@@ -2037,9 +2037,142 @@ void EmDee_displace(tEmDee* md, double lambda, double alpha, double dt) {
 
 void EmDee_move(tEmDee* md, double lambda, double alpha, double dt) { EmDee_displace(md, lambda, alpha, dt); }
 
+/* virtual_rotation of src/EmDeeCode.f90:1150-1163: a copy of the body takes
+ * pi + C(q) dt tau and rotates freely for dt; returns the copy's quaternion */
+static void virtual_rotation(const obody* b, double dt, int mode, double* qout) {
+  obody c = *b;
+  c.delta = (double*)xmalloc(sizeof(double) * 3 * (b->NP ? b->NP : 1));
+  memcpy(c.delta, b->delta, sizeof(double) * 3 * b->NP);
+  double v[3] = {dt * c.tau[0], dt * c.tau[1], dt * c.tau[2]}, t[4], pi[4];
+  matC(c.q, v, t);
+  for (int k = 0; k < 4; k++) pi[k] = c.pi[k] + t[k];
+  body_assign_pi(&c, pi);
+  if (mode != 0) rotate_no_squish(&c, dt, mode);
+  else rotate_exact(&c, dt);
+  for (int k = 0; k < 4; k++) qout[k] = c.q[k];
+  free(c.delta);
+}
+
+/* boost(me, thread, one, dt_2, me%F, TRUE, TRUE) of src/EmDeeData.f90:864-896 */
+static void verlet_boost(odata* me, double CF) {
+  const double* F = me->F;
+  for (int b = 0; b < me->nbodies; b++) {
+    obody* B = &me->body[b];
+    force_and_torque(B, F);
+    for (int d = 0; d < 3; d++) B->pcm[d] = 1.0 * B->pcm[d] + CF * B->F[d];
+    double Ctau = 2.0 * CF, v[3] = {Ctau * B->tau[0], Ctau * B->tau[1], Ctau * B->tau[2]}, c[4], pi[4];
+    matC(B->q, v, c);
+    for (int k = 0; k < 4; k++) pi[k] = 1.0 * B->pi[k] + c[k];
+    body_assign_pi(B, pi);
+  }
+  for (int q = 0; q < me->nfree; q++) {
+    int j = me->freeAtom[q] - 1;
+    for (int d = 0; d < 3; d++) me->P[3 * j + d] = 1.0 * me->P[3 * j + d] + CF * F[3 * j + d];
+  }
+}
+
+/* move(me, thread, one, dt, dt, TRUE, TRUE, mode) of src/EmDeeData.f90:823-860 */
+static void verlet_move(odata* me, double dt, int mode) {
+  for (int b = 0; b < me->nbodies; b++) {
+    obody* B = &me->body[b];
+    for (int d = 0; d < 3; d++) B->rcm[d] = 1.0 * B->rcm[d] + dt * B->invMass * B->pcm[d];
+  }
+  for (int q = 0; q < me->nfree; q++) {
+    int j = me->freeAtom[q] - 1;
+    for (int d = 0; d < 3; d++) me->R[3 * j + d] = 1.0 * me->R[3 * j + d] + dt * me->P[3 * j + d] * me->invMass[j];
+  }
+  for (int b = 0; b < me->nbodies; b++) {
+    obody* B = &me->body[b];
+    if (mode == 0) rotate_exact(B, dt);
+    else rotate_no_squish(B, dt, mode);
+    for (int k = 0; k < B->NP; k++)
+      for (int d = 0; d < 3; d++) me->R[3 * (B->index[k] - 1) + d] = B->rcm[d] + B->delta[3 * k + d];
+  }
+}
+
+/* src/EmDeeCode.f90:1107-1211 */
 void EmDee_verlet_step(tEmDee* md, double dt) {
-  (void)md; (void)dt;
-  error("verlet step", "not handled by the oracle");
+  odata* me = get(*md);
+  const double dt_2 = 0.5 * dt;
+  const int compute = md->Options.Compute, mode = md->Options.RotationMode;
+  const int nb = me->nbodies, nf = me->nfree;
+  double Us = 0.0, Ks_t = 0.0, Ks_r = 0.0;
+  double* r0 = (double*)xmalloc(sizeof(double) * 3 * (nb ? nb : 1));
+  double* q0 = (double*)xmalloc(sizeof(double) * 4 * (nb ? nb : 1));
+  double* s0 = (double*)xmalloc(sizeof(double) * 3 * (nf ? nf : 1));
+  /* pre_force */
+  if (compute) {
+    for (int b = 0; b < nb; b++) {
+      obody* B = &me->body[b];
+      double qv[4];
+      for (int d = 0; d < 3; d++) r0[3 * b + d] = 2.5 * B->rcm[d] + dt_2 * B->invMass * (B->pcm[d] - dt_2 * B->F[d]);
+      virtual_rotation(B, -dt, mode, qv);
+      for (int k = 0; k < 4; k++) q0[4 * b + k] = 0.5 * qv[k] - 3.0 * B->q[k];
+    }
+    for (int q = 0; q < nf; q++) {
+      int j = me->freeAtom[q] - 1;
+      for (int d = 0; d < 3; d++)
+        s0[3 * q + d] = 2.5 * me->R[3 * j + d] + dt_2 * me->invMass[j] * (me->P[3 * j + d] - dt_2 * me->F[3 * j + d]);
+    }
+  }
+  verlet_boost(me, dt_2);
+  verlet_move(me, dt, mode);
+  EmDee_compute_forces(md);   /* unconditional, and other layers keep their flags, as in the reference */
+  /* post_force */
+  verlet_boost(me, dt_2);
+  if (compute) {
+    double tk[3] = {0.0, 0.0, 0.0}, rk[3] = {0.0, 0.0, 0.0};
+    for (int b = 0; b < nb; b++)
+      for (int d = 0; d < 3; d++) tk[d] += me->body[b].invMass * (me->body[b].pcm[d] * me->body[b].pcm[d]);
+    for (int q = 0; q < nf; q++) {
+      int j = me->freeAtom[q] - 1;
+      for (int d = 0; d < 3; d++) tk[d] += me->invMass[j] * (me->P[3 * j + d] * me->P[3 * j + d]);
+    }
+    for (int b = 0; b < nb; b++)
+      for (int d = 0; d < 3; d++) rk[d] += me->body[b].MoI[d] * (me->body[b].omega[d] * me->body[b].omega[d]);
+    for (int b = 0; b < nb; b++) {
+      obody* B = &me->body[b];
+      double rdot[3], qdot[4], qv[4], dot = 0.0, t4[4], tb[3];
+      for (int d = 0; d < 3; d++) {
+        rdot[d] = 2.5 * B->rcm[d] + dt * B->invMass * (B->pcm[d] + dt_2 * B->F[d]) - r0[3 * b + d];
+        Ks_t += rdot[d] * B->pcm[d];
+      }
+      virtual_rotation(B, dt, mode, qv);
+      for (int k = 0; k < 4; k++) {
+        qdot[k] = q0[4 * b + k] + 1.5 * B->q[k] + qv[k];
+        dot += qdot[k] * B->q[k];
+      }
+      for (int k = 0; k < 4; k++) Ks_r += (qdot[k] - dot * B->q[k]) * B->pi[k];
+      matC(B->q, B->tau, t4);   /* tau_b = Bt C tau */
+      matBt(B->q, t4, tb);
+      Us += B->invMass * (B->F[0] * B->F[0] + B->F[1] * B->F[1] + B->F[2] * B->F[2]) +
+            (B->invMoI[0] * tb[0] * tb[0] + B->invMoI[1] * tb[1] * tb[1] + B->invMoI[2] * tb[2] * tb[2]);
+    }
+    for (int q = 0; q < nf; q++) {
+      int j = me->freeAtom[q] - 1;
+      const double* P = &me->P[3 * j];
+      const double* F = &me->F[3 * j];
+      for (int d = 0; d < 3; d++) {
+        double rdot = 2.5 * me->R[3 * j + d] + dt * me->invMass[j] * (P[d] + dt_2 * F[d]) - s0[3 * q + d];
+        Ks_t += rdot * P[d];
+      }
+      Us += me->invMass[j] * (F[0] * F[0] + F[1] * F[1] + F[2] * F[2]);
+    }
+    for (int d = 0; d < 3; d++) {
+      md->Kinetic.TransPart[d] = 0.5 * tk[d];
+      md->Kinetic.RotPart[d] = 0.5 * rk[d];
+    }
+    md->Kinetic.Rotational = md->Kinetic.RotPart[0] + md->Kinetic.RotPart[1] + md->Kinetic.RotPart[2];
+    md->Kinetic.Total = md->Kinetic.TransPart[0] + md->Kinetic.TransPart[1] + md->Kinetic.TransPart[2] +
+                        md->Kinetic.Rotational;
+    md->Energy.ShadowPotential = md->Energy.ShadowPotential - dt * dt * Us / 24.0;
+    md->Kinetic.ShadowRotational = Ks_r / (6.0 * dt);
+    md->Kinetic.ShadowKinetic = (Ks_t + Ks_r) / (6.0 * dt);
+  }
+  md->Kinetic.UpToDate = compute;
+  free(r0);
+  free(q0);
+  free(s0);
 }
 
 void EmDee_rdf(tEmDee md, int bins, double Rc, int pairs, int itype[], int jtype[], double g[]) {
