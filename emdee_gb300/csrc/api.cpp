@@ -1132,9 +1132,46 @@ void EmDee_verlet_step(tEmDee* md, double dt) {
   md->Kinetic.UpToDate = compute;
 }
 
+// src/EmDeeCode.f90:1281-1395: pair histograms over the current neighbor lists,
+// normalised by the ideal-gas shell counts in scaled units
 void EmDee_rdf(tEmDee md, int bins, double Rc, int pairs, int itype[], int jtype[], double g[]) {
-  (void)md; (void)bins; (void)Rc; (void)pairs; (void)itype; (void)jtype; (void)g;
-  fatal("radial distribution calculation", "not available in this build");
+  const char* task = "radial distribution calculation";
+  const double Pi4_3 = 4.188790204786391;
+  System& s = *sys_of(md);
+  MirrorScope scope(s);
+  const int nt = s.ntypes;
+  int maxtype = 0;
+  for (int p = 0; p < pairs; p++) {
+    if (itype[p] < 1 || itype[p] > nt || jtype[p] < 1 || jtype[p] > nt)
+      fatal(task, "at least one provided type index is out of range");
+    maxtype = std::max(maxtype, std::max(itype[p], jtype[p]));
+  }
+  if (!s.initialized || !s.r0Valid) fatal(task, "system has not been initialized");
+  if (bins < 1) fatal(task, "the number of bins must be positive");
+  std::vector<uint8_t> hasPair(nt, 0), pairOn((size_t)nt * nt, 0);
+  for (int p = 0; p < pairs; p++) {
+    hasPair[itype[p] - 1] = hasPair[jtype[p] - 1] = 1;
+    pairOn[(size_t)(itype[p] - 1) * nt + (jtype[p] - 1)] = 1;
+    pairOn[(size_t)(jtype[p] - 1) * nt + (itype[p] - 1)] = 1;
+  }
+  const int ntp = maxtype * (maxtype + 1) / 2;
+  std::vector<unsigned long long> counts;
+  device_rdf_counts(s, bins, Rc, hasPair, pairOn, ntp, counts);
+  const double invL = 1.0 / *s.Lbox, w = Rc * invL / bins;
+  for (int p = 0; p < pairs; p++) {
+    const int i = itype[p], j = jtype[p];
+    long long Ni = 0, Nj = 0;
+    for (int a = 0; a < s.natoms; a++) {
+      Ni += s.atomType[a] == i;
+      Nj += s.atomType[a] == j;
+    }
+    const int k = std::min(i, j) - 1 + std::max(i, j) * (std::max(i, j) - 1) / 2;   // symm1D - 1
+    for (int b = 1; b <= bins; b++) {
+      double rdf = (double)counts[(size_t)k * bins + b - 1] / (Pi4_3 * (w * w * w));
+      rdf = rdf / (3 * b * (b - 1) + 1);
+      g[(size_t)p * bins + b - 1] = (i == j ? 2.0 * rdf : rdf) / (double)(Ni * Nj);
+    }
+  }
 }
 
 void* EmDee_cuda_stream(tEmDee md) { return (void*)sys_of(md)->stream; }

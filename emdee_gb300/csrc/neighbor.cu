@@ -706,4 +706,124 @@ long device_neighbor_pairs(System& s, int* pairs, long capacity) {
   return n;
 }
 
+// ---------------------------------------------------------------------------------
+// radial distribution histograms over the current lists (src/EmDeeCode.f90:1281-1395)
+// ---------------------------------------------------------------------------------
+
+struct RdfArgs {
+  TileGeom g;
+  const int2* tab;
+  const int* start;
+  const int* orig;
+  const uint16_t* nb;
+  const int* count;   // entries to scan per slot (all, or the inner part)
+  const uint8_t* type8;
+  const double* R;
+  int cap, tileStride, bins, ntp;   // ntp: histogram rows (type pairs, symm1D order)
+  double invL, Rc2, binsByRc;
+  const uint8_t* hasPair;   // [type] (0-based)
+  const uint8_t* pairOn;    // [ti * ntypes + tj]
+  int ntypes, haloCap;
+  unsigned long long* hist;   // [pair][bin], every pair counted from both of its atoms
+  int sharedHist;             // histogram fits in shared memory
+};
+
+__global__ void k_rdf(RdfArgs A) {
+  extern __shared__ int dyn[];
+  __shared__ int ws[33];
+  __shared__ int off[1001], cst[1000];
+  const TileGeom g = A.g;
+  const int t = blockIdx.x, cells = g.TB * g.TB * g.TB;
+  int* hslot = dyn;   // halo index -> slot, then the block's histogram
+  halo_layout(g, t, A.tab, A.start, off, cst, (int*)nullptr, ws);
+  unsigned int* sh = (unsigned int*)(hslot + A.haloCap);
+  for (int h = threadIdx.x; h < g.haloCells; h += blockDim.x)
+    for (int k = off[h]; k < off[h + 1]; k++) hslot[k] = cst[h] + (k - off[h]);
+  const int hn = A.bins * A.ntp;
+  if (A.sharedHist)
+    for (int k = threadIdx.x; k < hn; k += blockDim.x) sh[k] = 0u;
+  __syncthreads();
+  const int tb = A.start[t * cells], te = A.start[(t + 1) * cells];
+  for (int li = threadIdx.x; li < te - tb; li += blockDim.x) {
+    const int si = tb + li, ai = A.orig[si], ti = A.type8[si];
+    if (!A.hasPair[ti]) continue;
+    const double xi = A.invL * A.R[3 * ai], yi = A.invL * A.R[3 * ai + 1], zi = A.invL * A.R[3 * ai + 2];
+    const int n = A.count[si];
+    for (int k = 0; k < n; k++) {
+      const int q = A.nb[nb_index(t, A.cap >> 3, A.tileStride, li, k)];
+      const int sj = hslot[q], aj = A.orig[sj], tj = A.type8[sj];
+      if (!A.pairOn[ti * A.ntypes + tj]) continue;
+      double dx = xi - A.invL * A.R[3 * aj], dy = yi - A.invL * A.R[3 * aj + 1], dz = zi - A.invL * A.R[3 * aj + 2];
+      dx = dx - round(dx);
+      dy = dy - round(dy);
+      dz = dz - round(dz);
+      const double r2 = dx * dx + dy * dy + dz * dz;
+      if (r2 < A.Rc2) {
+        int bin = (int)(sqrt(r2) * A.binsByRc);
+        bin = min(bin, A.bins - 1);
+        const int a = min(ti, tj), b = max(ti, tj), p = a + (b + 1) * b / 2;   // symm1D - 1 (0-based types)
+        if (A.sharedHist) atomicAdd(&sh[p * A.bins + bin], 1u);
+        else atomicAdd(&A.hist[(size_t)p * A.bins + bin], 1ull);
+      }
+    }
+  }
+  if (A.sharedHist) {
+    __syncthreads();
+    for (int k = threadIdx.x; k < hn; k += blockDim.x)
+      if (sh[k]) atomicAdd(&A.hist[k], (unsigned long long)sh[k]);
+  }
+}
+
+// counts[pair][bin] (pairs in symm1D order over types 1..maxtype), each pair once
+void device_rdf_counts(System& s, int bins, double Rc, const std::vector<uint8_t>& hasPair,
+                       const std::vector<uint8_t>& pairOn, int ntp, std::vector<unsigned long long>& counts) {
+  Grid& g = s.grid;
+  const int nt = s.ntypes;
+  RdfArgs A;
+  A.g = make_geom(g.M, g.TB);
+  A.tab = g.dHaloTab;
+  A.start = g.dStart;
+  A.orig = g.dOrig;
+  A.nb = g.dNb;
+  A.count = Rc < 1.0001 * s.InRc ? g.dNbInner : g.dNbCount;
+  A.type8 = g.dType8;
+  A.R = s.dR;
+  A.cap = g.cap;
+  A.tileStride = g.tileStride;
+  A.bins = bins;
+  A.ntp = ntp;
+  const double invL = 1.0 / *s.Lbox;
+  A.invL = invL;
+  A.Rc2 = Rc * Rc * (invL * invL);
+  A.binsByRc = bins / (Rc * invL);
+  A.ntypes = nt;
+  A.haloCap = g.maxHalo;
+  const size_t hn = (size_t)bins * ntp;
+  uint8_t *dHas, *dOn;
+  unsigned long long* dHist;
+  CK(cudaMalloc(&dHas, nt));
+  CK(cudaMalloc(&dOn, (size_t)nt * nt));
+  CK(cudaMalloc(&dHist, sizeof(unsigned long long) * hn));
+  CK(cudaMemcpy(dHas, hasPair.data(), nt, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(dOn, pairOn.data(), (size_t)nt * nt, cudaMemcpyHostToDevice));
+  CK(cudaMemsetAsync(dHist, 0, sizeof(unsigned long long) * hn, s.stream));
+  A.hasPair = dHas;
+  A.pairOn = dOn;
+  A.hist = dHist;
+  size_t smem = sizeof(int) * (size_t)g.maxHalo;
+  A.sharedHist = (hn * sizeof(unsigned int) <= 48 * 1024) ? 1 : 0;
+  if (A.sharedHist) smem += hn * sizeof(unsigned int);
+  CK(cudaFuncSetAttribute(k_rdf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_rdf<<<g.nTiles, 128, smem, s.stream>>>(A);
+  CK(cudaGetLastError());
+  s.prof.total++;
+  counts.assign(hn, 0ull);
+  CK(cudaStreamSynchronize(s.stream));
+  CK(cudaMemcpy(counts.data(), dHist, sizeof(unsigned long long) * hn, cudaMemcpyDeviceToHost));
+  for (auto& c : counts) c /= 2;   // full lists hold every pair twice, at the same distance
+  CK(cudaFree(dHas));
+  CK(cudaFree(dOn));
+  CK(cudaFree(dHist));
+}
+
 }  // namespace emdee

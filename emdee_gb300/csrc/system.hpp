@@ -265,6 +265,9 @@ long device_neighbor_pairs(System& s, int* pairs, long capacity);
 void ewald_initialize(System& s, double kspaceRc);
 double ewald_compute(System& s);
 void ewald_free(System& s);
+// EmDee_rdf histograms over the current lists (neighbor.cu)
+void device_rdf_counts(System& s, int bins, double Rc, const std::vector<uint8_t>& hasPair,
+                       const std::vector<uint8_t>& pairOn, int ntp, std::vector<unsigned long long>& counts);
 // EmDee_verlet_step halves (verlet.cu)
 void device_verlet_pre(System& s, double dt, bool compute, int mode);
 void device_verlet_post(System& s, double dt, bool compute, int mode, double* out);

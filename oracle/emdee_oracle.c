@@ -2175,9 +2175,71 @@ void EmDee_verlet_step(tEmDee* md, double dt) {
   free(s0);
 }
 
+/* src/EmDeeCode.f90:1281-1395: pair histograms over the current neighbor lists */
 void EmDee_rdf(tEmDee md, int bins, double Rc, int pairs, int itype[], int jtype[], double g[]) {
-  (void)md; (void)bins; (void)Rc; (void)pairs; (void)itype; (void)jtype; (void)g;
-  error("radial distribution calculation", "not handled by the oracle");
+  const char* task = "radial distribution calculation";
+  const double Pi4_3 = 4.188790204786391;
+  odata* me = get(md);
+  int nt = me->ntypes, maxtype = 0;
+  for (int p = 0; p < pairs; p++) {
+    if (!ranged(itype[p], nt) || !ranged(jtype[p], nt)) error(task, "at least one provided type index is out of range");
+    if (itype[p] > maxtype) maxtype = itype[p];
+    if (jtype[p] > maxtype) maxtype = jtype[p];
+  }
+  char* hasPair = (char*)xcalloc(nt + 1, 1);
+  char* pairOn = (char*)xcalloc((size_t)(nt + 1) * (nt + 1), 1);
+  for (int p = 0; p < pairs; p++) {
+    hasPair[itype[p]] = hasPair[jtype[p]] = 1;
+    pairOn[itype[p] * (nt + 1) + jtype[p]] = pairOn[jtype[p] * (nt + 1) + itype[p]] = 1;
+  }
+  int npt = symm1D(maxtype, maxtype);
+  long* count = (long*)xcalloc((size_t)bins * npt, sizeof(long));
+  double invL = 1.0 / *me->Lbox, invL2 = invL * invL;
+  double* Rs = (double*)xmalloc(sizeof(double) * 3 * me->natoms);
+  for (size_t q = 0; q < (size_t)3 * me->natoms; q++) Rs[q] = invL * me->R[q];
+  double Rc2 = Rc * Rc * invL2, binsByRc = bins / (Rc * invL);
+  for (int t = 0; t < me->nthreads; t++) {
+    olist* nb = &me->neighbor[t];
+    int* last = Rc < 1.0001 * me->InRc ? nb->middle : nb->last;
+    for (int c = me->threadCellFirst[t]; c <= me->threadCellLast[t]; c++)
+      for (int k = me->cellFirst[c - 1]; k <= me->cellLast[c - 1]; k++) {
+        int i = me->cellItem[k - 1], ti = me->atomType[i - 1];
+        if (!hasPair[ti]) continue;
+        for (int m = nb->first[i - 1]; m <= last[i - 1]; m++) {
+          int j = nb->item[m - 1], tj = me->atomType[j - 1];
+          if (!pairOn[ti * (nt + 1) + tj]) continue;
+          double r2 = 0.0;
+          for (int d = 0; d < 3; d++) {
+            double x = Rs[3 * (i - 1) + d] - Rs[3 * (j - 1) + d];
+            x = x - anint(x);
+            r2 += x * x;
+          }
+          if (r2 < Rc2) {
+            int bin = (int)(sqrt(r2) * binsByRc);
+            if (bin > bins - 1) bin = bins - 1;   /* rounding at r -> Rc; the reference would index past the end */
+            count[(size_t)(symm1D(ti, tj) - 1) * bins + bin]++;
+          }
+        }
+      }
+  }
+  for (int p = 0; p < pairs; p++) {
+    int i = itype[p], j = jtype[p];
+    long Ni = 0, Nj = 0;
+    for (int a = 0; a < me->natoms; a++) {
+      Ni += me->atomType[a] == i;
+      Nj += me->atomType[a] == j;
+    }
+    for (int b = 1; b <= bins; b++) {
+      double w = Rc * invL / bins;
+      double rdf = (double)count[(size_t)(symm1D(i, j) - 1) * bins + b - 1] / (Pi4_3 * (w * w * w));
+      rdf = rdf / (3 * b * (b - 1) + 1);
+      g[(size_t)p * bins + b - 1] = (i == j ? 2.0 * rdf : rdf) / (double)(Ni * Nj);
+    }
+  }
+  free(hasPair);
+  free(pairOn);
+  free(count);
+  free(Rs);
 }
 
 /* pairs of the current neighbor lists, (min,max) 1-based, sorted */
