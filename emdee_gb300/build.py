@@ -32,6 +32,7 @@ UNITS = {
     "bodies.cu": ["-fmad=false"],
     "ewald.cu": ["-fmad=false"],
     "verlet.cu": ["-fmad=false"],
+    "replicas.cu": ["-fmad=false"],
 }
 HEADERS = ["system.hpp", "pairmath.cuh", "tile.cuh", "reduce.cuh", "rigid.cuh", "bodies.cuh", os.path.join("..", "..", "include", "emdee.h")]
 

@@ -1,0 +1,617 @@
+// replicas.cu -- many independent systems advanced together by one persistent
+// kernel (no reference counterpart: the reference runs one system per call).
+//
+// One thread block owns one replica for the whole run: every step it performs,
+// with block-wide barriers between the phases, the reference's velocity-Verlet
+// loop body (test/common/contained.f90:63-72) -- boost(dt/2), displace(dt),
+// the skin check of src/neighbor_lists.f90:41-59, a neighbor-list rebuild when
+// it fires, the pair forces, boost(dt/2) -- so a whole trajectory of hundreds of
+// replicas is one launch (captured once in a CUDA graph and replayed).
+//
+// Per replica, in shared memory: the FP32 positions of its atoms in cell units
+// relative to each atom's cell at the last build (slot order), the cell starts
+// and the 125 stencil offsets.  In global memory: R, P, F, R0 of the system
+// (FP64, API order) and the replica's own cell-sorted order, build-time cells
+// and full neighbor lists (column-major, 32-bit entries: slot | stencil code).
+// Blocks are issued largest replica first.
+//
+// Scope: single atom type, no charges, no rigid bodies, no exclusions, one
+// model layer, FP32 pair arithmetic (the mixed mode).  The pair set is the
+// reference's: FP32 prefilter, FP64 test of src/neighbor_lists.f90:247-250 for
+// candidates within 4e-5 of the threshold (this file uses -fmad=false).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "reduce.cuh"
+#include "system.hpp"
+#include "tile.cuh"
+
+namespace emdee {
+
+struct RepDesc {
+  double *R, *P, *F, *R0;        // the system's arrays (API order)
+  const double* invMass;
+  int unitMass;
+  int N, M, minimg, cap;
+  double L, scale, skinSq, thr;   // scale = M / L; thr = (rc+skin)^2 / L^2
+  float lo2, hi2, rc2, invw2, invw, Mf;
+  PairEntry<float> model;
+  int* orig;        // slot -> atom
+  int4* K;          // per slot: build-time unwrapped cell (x, y, z), cell rank (w)
+  int4* atomK;      // per atom scratch of the same
+  uint32_t* list;   // entry n of slot i at list[n * N + i]
+  int* count;       // per slot
+  double* out;      // [0] Epair [1] Wpair [2..4] 2KE per dim [5] builds [6] overflow [7] steps done
+  int computeLast;  // unused by the kernel (host bookkeeping)
+};
+
+static const double REP_BAND = 4e-5;
+
+__device__ __forceinline__ bool rep_exact_inside(const double* R, double L, int a, int b, double thr) {
+  double d[3];
+  for (int k = 0; k < 3; k++) {
+    double x = R[3 * a + k] / L - R[3 * b + k] / L;
+    d[k] = x - round(x);
+  }
+  return d[0] * d[0] + d[1] * d[1] + d[2] * d[2] < thr;
+}
+
+// (max, prev) combine of the skin check over contiguous index ranges (see neighbor.cu)
+struct RepMP {
+  long long m, p;
+};
+__device__ __forceinline__ RepMP rep_combine(RepMP a, RepMP b) {
+  if (b.m > a.m) return RepMP{b.m, a.m > b.p ? a.m : b.p};
+  return a;
+}
+__device__ __forceinline__ RepMP rep_warp_ordered(RepMP acc) {
+  const int lane = threadIdx.x & 31;
+  for (int o = 1; o < 32; o <<= 1) {
+    RepMP other{(long long)__shfl_down_sync(0xffffffffu, (unsigned long long)acc.m, o),
+                (long long)__shfl_down_sync(0xffffffffu, (unsigned long long)acc.p, o)};
+    if ((lane & (2 * o - 1)) == 0) acc = rep_combine(acc, other);
+  }
+  return acc;
+}
+
+// cell and unwrapped cell of an atom (src/neighbor_lists.f90:126-127, index clamped to M-1)
+__device__ __forceinline__ int4 rep_cell(const double* R, int a, double L, int M) {
+  int c[3], K[3];
+  for (int d = 0; d < 3; d++) {
+    double rs = R[3 * a + d] / L, fl = floor(rs);
+    int ci = (int)(M * (rs - fl));
+    ci = ci < 0 ? 0 : (ci >= M ? M - 1 : ci);
+    c[d] = ci;
+    K[d] = (int)fl * M + ci;
+  }
+  return make_int4(K[0], K[1], K[2], c[0] + M * (c[1] + M * c[2]));
+}
+
+struct RepShared {
+  RepDesc d;
+  int rebuild, overflow;
+  RepMP wmp[32];
+  float2 wff[2][32];
+  double wke[3][32];
+};
+
+template <int THREADS>
+__device__ void rep_build(RepShared& S, const double* Rb, float4* pos, int* cellStart, int* cursor,
+                          const float4* offTab, bool copyR0) {
+  const RepDesc& D = S.d;
+  const int N = D.N, M = D.M, cells = M * M * M;
+  for (int c = threadIdx.x; c < cells; c += THREADS) cursor[c] = 0;
+  __syncthreads();
+  for (int a = threadIdx.x; a < N; a += THREADS) {
+    const int4 k = rep_cell(Rb, a, D.L, M);
+    D.atomK[a] = k;
+    atomicAdd(&cursor[k.w], 1);
+  }
+  __syncthreads();
+  // exclusive scan of the cell counts into cellStart (a single warp walks the cells)
+  if (threadIdx.x < 32) {
+    int carry = 0;
+    for (int base = 0; base < cells; base += 32) {
+      const int c = base + threadIdx.x;
+      const int v = c < cells ? cursor[c] : 0;
+      int incl = v;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if ((int)threadIdx.x >= o) incl += y;
+      }
+      if (c < cells) cellStart[c] = carry + incl - v;
+      carry += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    if (threadIdx.x == 0) cellStart[cells] = carry;
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < cells; c += THREADS) cursor[c] = 0;
+  __syncthreads();
+  for (int a = threadIdx.x; a < N; a += THREADS) {
+    const int r = D.atomK[a].w;
+    D.orig[cellStart[r] + atomicAdd(&cursor[r], 1)] = a;
+  }
+  __syncthreads();
+  // deterministic order inside a cell: ascending atom index
+  for (int c = threadIdx.x; c < cells; c += THREADS) {
+    const int b = cellStart[c], e = cellStart[c + 1];
+    for (int i = b + 1; i < e; i++) {
+      const int v = D.orig[i];
+      int j = i - 1;
+      while (j >= b && D.orig[j] > v) {
+        D.orig[j + 1] = D.orig[j];
+        j--;
+      }
+      D.orig[j + 1] = v;
+    }
+  }
+  __syncthreads();
+  for (int s = threadIdx.x; s < N; s += THREADS) {
+    const int a = D.orig[s];
+    const int4 k = D.atomK[a];
+    D.K[s] = k;
+    pos[s] = make_float4((float)(Rb[3 * a] * D.scale - (double)k.x), (float)(Rb[3 * a + 1] * D.scale - (double)k.y),
+                         (float)(Rb[3 * a + 2] * D.scale - (double)k.z), 0.f);
+  }
+  __syncthreads();
+  // full lists: 125 stencil cells, candidate order (z, y, x, slot)
+  for (int i = threadIdx.x; i < N; i += THREADS) {
+    const int4 ki = D.K[i];
+    const int cx = ki.w % M, cy = (ki.w / M) % M, cz = ki.w / (M * M);
+    const float4 pi = pos[i];
+    const int ai = D.orig[i];
+    int n = 0;
+    for (int code = 0; code < 125; code++) {
+      const int sx = code % 5 - 2, sy = (code / 5) % 5 - 2, sz = code / 25 - 2;
+      const int nc = wrap(cx + sx, M) + M * (wrap(cy + sy, M) + M * wrap(cz + sz, M));
+      const float4 o = offTab[code];
+      for (int j = cellStart[nc]; j < cellStart[nc + 1]; j++) {
+        if (j == i) continue;
+        const float4 pj = pos[j];
+        float dx = (pi.x - pj.x) - o.x, dy = (pi.y - pj.y) - o.y, dz = (pi.z - pj.z) - o.z;
+        if (D.minimg) {
+          dx -= D.Mf * rintf(dx / D.Mf);
+          dy -= D.Mf * rintf(dy / D.Mf);
+          dz -= D.Mf * rintf(dz / D.Mf);
+        }
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        if (r2 >= D.hi2) continue;
+        if (!(r2 < D.lo2) && !rep_exact_inside(Rb, D.L, ai, D.orig[j], D.thr)) continue;
+        if (n < D.cap) D.list[(size_t)n * N + i] = (uint32_t)j | ((uint32_t)code << 16);
+        n++;
+      }
+    }
+    D.count[i] = n;
+    if (n > D.cap) atomicMax(&S.overflow, n);
+  }
+  if (copyR0)
+    for (int q = threadIdx.x; q < 3 * N; q += THREADS) D.R0[q] = D.R[q];
+  __syncthreads();
+}
+
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS) k_replicas(const RepDesc* __restrict__ descs, const int* __restrict__ order,
+                                                      int steps, double dt, int nprop, int Nmax, int cellsMax) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ RepShared S;
+  float4* pos = (float4*)smem;
+  float4* offTab = pos + Nmax;
+  int* cellStart = (int*)(offTab + 125);
+  int* cursor = cellStart + cellsMax + 1;
+  if (threadIdx.x == 0) {
+    S.d = descs[order[blockIdx.x]];
+    S.overflow = 0;
+  }
+  for (int c = threadIdx.x; c < 125; c += THREADS)
+    offTab[c] = make_float4((float)(c % 5 - 2), (float)((c / 5) % 5 - 2), (float)(c / 25 - 2), 0.f);
+  __syncthreads();
+  const RepDesc& D = S.d;
+  const int N = D.N, lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = THREADS / 32;
+  const double dt_2 = 0.5 * dt;
+  int done = (int)D.out[7];
+  // lists as the system's were built: from the positions of the last build (R0)
+  rep_build<THREADS>(S, D.R0, pos, cellStart, cursor, offTab, false);
+  double builds = D.out[5];
+  for (int k = 0; k < steps; k++) {
+    const bool compute = (done + k + 1) % nprop == 0;
+    // boost(dt/2) and displace(dt), FP64 (src/EmDeeData.f90:823-896)
+    for (int a = threadIdx.x; a < N; a += THREADS) {
+      const double im = D.unitMass ? 1.0 : D.invMass[a];
+      for (int d = 0; d < 3; d++) {
+        const double p = D.P[3 * a + d] + dt_2 * D.F[3 * a + d];
+        D.P[3 * a + d] = p;
+        D.R[3 * a + d] = D.unitMass ? D.R[3 * a + d] + dt * p : D.R[3 * a + d] + dt * p * im;
+      }
+    }
+    __syncthreads();
+    // skin check over atoms in index order: warp w takes a contiguous range
+    {
+      const int per = (N + nw - 1) / nw, a0 = warp * per, a1 = min(N, a0 + per);
+      RepMP run{-1, -1};
+      for (int base = a0; base < a1; base += 32) {
+        const int a = base + lane;
+        RepMP v{-1, -1};
+        if (a < a1) {
+          const double d0 = D.R[3 * a] - D.R0[3 * a], d1 = D.R[3 * a + 1] - D.R0[3 * a + 1],
+                       d2 = D.R[3 * a + 2] - D.R0[3 * a + 2];
+          v.m = __double_as_longlong(d0 * d0 + d1 * d1 + d2 * d2);
+        }
+        v = rep_warp_ordered(v);
+        run = rep_combine(run, v);
+      }
+      if (lane == 0) S.wmp[warp] = run;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        RepMP b = S.wmp[0];
+        for (int w = 1; w < nw; w++) b = rep_combine(b, S.wmp[w]);
+        const double mx = __longlong_as_double(b.m), nx = __longlong_as_double(b.p < 0 ? b.m : b.p);
+        S.rebuild = mx + 2 * sqrt(mx * nx) + nx > D.skinSq;
+      }
+      __syncthreads();
+    }
+    if (S.rebuild) {
+      rep_build<THREADS>(S, D.R, pos, cellStart, cursor, offTab, true);
+      builds += 1.0;
+    }
+    // positions in cell units relative to the build-time cells
+    for (int s = threadIdx.x; s < N; s += THREADS) {
+      const int a = D.orig[s];
+      const int4 kk = D.K[s];
+      pos[s] = make_float4((float)(D.R[3 * a] * D.scale - (double)kk.x), (float)(D.R[3 * a + 1] * D.scale - (double)kk.y),
+                           (float)(D.R[3 * a + 2] * D.scale - (double)kk.z), 0.f);
+    }
+    __syncthreads();
+    // pair forces (full lists, no atomics); energies on compute steps, virial every step
+    float Ep = 0.f, Wp = 0.f;
+    {
+      const NBParams<float> mdl = D.model.model;
+      const float rc2 = D.rc2, invw2 = D.invw2, invw = D.invw, Mf = D.Mf;
+      const bool minimg = D.minimg;
+      const int cap = D.cap;
+      const uint32_t* __restrict__ list = D.list;
+      const int* __restrict__ count = D.count;
+      const int* __restrict__ orig = D.orig;
+      double* __restrict__ F = D.F;
+      for (int i = threadIdx.x; i < N; i += THREADS) {
+        const float4 pi = pos[i];
+        const int n = min(count[i], cap);
+        float fx = 0.f, fy = 0.f, fz = 0.f;
+        for (int q = 0; q < n; q++) {
+          const uint32_t e = __ldg(&list[(size_t)q * N + i]);
+          const float4 pj = pos[e & 0xFFFFu];
+          const float4 o = offTab[e >> 16];
+          float dx = (pi.x - pj.x) - o.x, dy = (pi.y - pj.y) - o.y, dz = (pi.z - pj.z) - o.z;
+          if (minimg) {
+            dx -= Mf * rintf(dx / Mf);
+            dy -= Mf * rintf(dy / Mf);
+            dz -= Mf * rintf(dz / Mf);
+          }
+          const float r2 = dx * dx + dy * dy + dz * dz;
+          const bool in = r2 < rc2;
+          const float invR2c = Ops<float>::rcp(r2), invR2 = invR2c * invw2, invR = sqrtf(invR2);
+          float E, W;
+          nb_compute(mdl, E, W, invR, invR2);
+          modifier_compute(mdl, E, W, invR, invR2);
+          W = in ? W : 0.f;
+          Ep += in ? E : 0.f;
+          Wp += W;
+          const float sc = W * invR2c;
+          fx += sc * dx;
+          fy += sc * dy;
+          fz += sc * dz;
+        }
+        const int a = orig[i];
+        F[3 * a] = f2d_exact(fx * invw);
+        F[3 * a + 1] = f2d_exact(fy * invw);
+        F[3 * a + 2] = f2d_exact(fz * invw);
+      }
+    }
+    {
+      float hi[2] = {0.5f * Ep, 0.5f * Wp}, lo[2] = {0.f, 0.f};
+      warp_sum_ff<2>(hi, lo);
+      if (lane == 0) {
+        S.wff[0][warp] = make_float2(hi[0], lo[0]);
+        S.wff[1][warp] = make_float2(hi[1], lo[1]);
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x < 2) {
+      float h = 0.f, l = 0.f;
+      for (int w = 0; w < nw; w++) ff_add(h, l, S.wff[threadIdx.x][w].x, S.wff[threadIdx.x][w].y);
+      if (threadIdx.x == 1 || compute) D.out[threadIdx.x] = (double)h + (double)l;
+    }
+    // boost(dt/2) with the new forces; kinetic energies on compute steps
+    double ke[3] = {0.0, 0.0, 0.0};
+    for (int a = threadIdx.x; a < N; a += THREADS) {
+      const double im = D.unitMass ? 1.0 : D.invMass[a];
+      for (int d = 0; d < 3; d++) {
+        const double p = D.P[3 * a + d] + dt_2 * D.F[3 * a + d];
+        D.P[3 * a + d] = p;
+        if (compute) ke[d] += im * (p * p);
+      }
+    }
+    if (compute) {
+      for (int d = 0; d < 3; d++)
+        for (int o = 16; o > 0; o >>= 1) ke[d] += __shfl_down_sync(0xffffffffu, ke[d], o);
+      if (lane == 0)
+        for (int d = 0; d < 3; d++) S.wke[d][warp] = ke[d];
+    }
+    __syncthreads();
+    if (compute && threadIdx.x < 3) {
+      double x = 0.0;
+      for (int w = 0; w < nw; w++) x += S.wke[threadIdx.x][w];
+      D.out[2 + threadIdx.x] = x;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    D.out[5] = builds;
+    D.out[6] = (double)S.overflow;
+    D.out[7] = (double)(done + steps);
+  }
+}
+
+// ---- host -----------------------------------------------------------------------
+
+struct Replicas {
+  std::vector<tEmDee*> md;
+  std::vector<System*> sys;
+  std::vector<RepDesc> desc;
+  RepDesc* dDesc = nullptr;
+  int* dOrder = nullptr;
+  double* dOut = nullptr;
+  double* hOut = nullptr;
+  std::vector<void*> owned;
+  int n = 0, Nmax = 0, cellsMax = 0, threads = 0;
+  size_t smem = 0;
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  int gSteps = -1, gNprop = -1;
+  double gDt = 0.0;
+  int steps = 0;
+};
+
+static void rep_launch(Replicas& B, int steps, double dt, int nprop, cudaStream_t st) {
+  switch (B.threads) {
+    case 256:
+      k_replicas<256><<<B.n, 256, B.smem, st>>>(B.dDesc, B.dOrder, steps, dt, nprop, B.Nmax, B.cellsMax);
+      break;
+    case 512:
+      k_replicas<512><<<B.n, 512, B.smem, st>>>(B.dDesc, B.dOrder, steps, dt, nprop, B.Nmax, B.cellsMax);
+      break;
+    default:
+      k_replicas<1024><<<B.n, 1024, B.smem, st>>>(B.dDesc, B.dOrder, steps, dt, nprop, B.Nmax, B.cellsMax);
+      break;
+  }
+  CK(cudaGetLastError());
+}
+
+static void rep_set_smem(Replicas& B) {
+  CK(cudaFuncSetAttribute(k_replicas<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)B.smem));
+  CK(cudaFuncSetAttribute(k_replicas<512>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)B.smem));
+  CK(cudaFuncSetAttribute(k_replicas<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)B.smem));
+}
+
+// Chooses the block size by timing a few steps of every candidate on scratch
+// copies of the replicas' state (the systems themselves are not touched).
+static int rep_autotune(Replicas& B, double dt, int nprop) {
+  std::vector<RepDesc> scratch = B.desc;
+  std::vector<void*> tmp;
+  for (int r = 0; r < B.n; r++) {
+    RepDesc& d = scratch[r];
+    size_t b3 = sizeof(double) * 3 * d.N;
+    double *R, *P, *F, *R0, *out;
+    CK(cudaMalloc(&R, b3));
+    CK(cudaMalloc(&P, b3));
+    CK(cudaMalloc(&F, b3));
+    CK(cudaMalloc(&R0, b3));
+    CK(cudaMalloc(&out, sizeof(double) * 8));
+    CK(cudaMemcpyAsync(R, d.R, b3, cudaMemcpyDeviceToDevice, B.stream));
+    CK(cudaMemcpyAsync(P, d.P, b3, cudaMemcpyDeviceToDevice, B.stream));
+    CK(cudaMemcpyAsync(F, d.F, b3, cudaMemcpyDeviceToDevice, B.stream));
+    CK(cudaMemcpyAsync(R0, d.R0, b3, cudaMemcpyDeviceToDevice, B.stream));
+    CK(cudaMemcpyAsync(out, d.out, sizeof(double) * 8, cudaMemcpyDeviceToDevice, B.stream));
+    d.R = R;
+    d.P = P;
+    d.F = F;
+    d.R0 = R0;
+    d.out = out;
+    tmp.insert(tmp.end(), {R, P, F, R0, out});
+  }
+  RepDesc* dScratch;
+  CK(cudaMalloc(&dScratch, sizeof(RepDesc) * B.n));
+  CK(cudaMemcpyAsync(dScratch, scratch.data(), sizeof(RepDesc) * B.n, cudaMemcpyHostToDevice, B.stream));
+  RepDesc* keep = B.dDesc;
+  B.dDesc = dScratch;
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  int best = 1024;
+  float bestMs = 1e30f;
+  for (int th : {256, 512, 1024}) {
+    B.threads = th;
+    rep_launch(B, 2, dt, nprop, B.stream);   // warm-up
+    CK(cudaEventRecord(e0, B.stream));
+    rep_launch(B, 10, dt, nprop, B.stream);
+    CK(cudaEventRecord(e1, B.stream));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    if (ms < bestMs) {
+      bestMs = ms;
+      best = th;
+    }
+  }
+  CK(cudaEventDestroy(e0));
+  CK(cudaEventDestroy(e1));
+  B.dDesc = keep;
+  CK(cudaFree(dScratch));
+  for (void* p : tmp) CK(cudaFree(p));
+  return best;
+}
+
+}  // namespace emdee
+
+using namespace emdee;
+
+extern "C" {
+
+void* EmDee_replicas_create(int n, tEmDee** systems) {
+  const char* task = "replica batch setup";
+  if (n < 1 || !systems) fatal(task, "at least one system is required");
+  Replicas* B = new Replicas;
+  B->n = n;
+  CK(cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking));
+  CK(cudaMalloc(&B->dOut, sizeof(double) * 8 * n));
+  CK(cudaMallocHost(&B->hOut, sizeof(double) * 8 * n));
+  CK(cudaMemset(B->dOut, 0, sizeof(double) * 8 * n));
+  std::vector<int> order(n);
+  for (int r = 0; r < n; r++) {
+    tEmDee* md = systems[r];
+    System& s = *sys_of(*md);
+    if (!s.initialized) fatal(task, "every system must be initialized (box and coordinates uploaded)");
+    if (s.ntypes != 1 || s.nbodies > 0 || s.hasExclusions || s.nlayers != 1 || s.precision != 0)
+      fatal(task, "replicas must have one atom type, no bodies, no exclusions, one layer and mixed precision");
+    for (int a = 0; a < s.natoms; a++)
+      if (s.charged[a]) fatal(task, "replicas must carry no charges");
+    if (s.natoms > 65535) fatal(task, "replicas are limited to 65535 atoms");
+    CK(cudaStreamSynchronize(s.stream));
+    RepDesc d;
+    memset(&d, 0, sizeof d);
+    d.R = s.dR;
+    d.P = s.dP;
+    d.F = s.F();
+    d.R0 = s.dR0;
+    d.invMass = s.dInvMass;
+    d.unitMass = s.unitMass ? 1 : 0;
+    d.N = s.natoms;
+    const double L = *s.Lbox;
+    d.M = std::max((int)std::floor(2.0 * L / s.xRc), 5);
+    d.minimg = d.M == 5;
+    d.L = L;
+    d.scale = d.M / L;
+    d.skinSq = s.skinSq;
+    d.thr = s.xRcSq / (L * L);
+    const double M2 = (double)d.M * d.M;
+    d.lo2 = (float)(d.thr * M2 * (1.0 - REP_BAND));
+    d.hi2 = (float)(d.thr * M2 * (1.0 + REP_BAND));
+    d.rc2 = (float)(s.RcSq / (L * L) * M2);
+    const double w = L / d.M;
+    d.invw2 = (float)(1.0 / (w * w));
+    d.invw = (float)(1.0 / w);
+    d.Mf = (float)d.M;
+    CK(cudaMemcpy(&d.model, s.models.d32, sizeof(PairEntry<float>), cudaMemcpyDeviceToHost));
+    // list capacity: twice the ideal-gas count within rc+skin, at least 64
+    const double expect = 4.0 / 3.0 * 3.14159265358979 * std::pow(s.xRc, 3) * s.natoms / (L * L * L);
+    d.cap = std::max(64, ((int)(2.0 * expect) + 7) / 8 * 8);
+    CK(cudaMalloc(&d.orig, sizeof(int) * d.N));
+    CK(cudaMalloc(&d.K, sizeof(int4) * d.N));
+    CK(cudaMalloc(&d.atomK, sizeof(int4) * d.N));
+    CK(cudaMalloc(&d.list, sizeof(uint32_t) * (size_t)d.cap * d.N));
+    CK(cudaMalloc(&d.count, sizeof(int) * d.N));
+    B->owned.insert(B->owned.end(), {d.orig, d.K, d.atomK, d.list, d.count});
+    d.out = B->dOut + 8 * r;
+    B->desc.push_back(d);
+    B->md.push_back(md);
+    B->sys.push_back(&s);
+    B->Nmax = std::max(B->Nmax, d.N);
+    B->cellsMax = std::max(B->cellsMax, d.M * d.M * d.M);
+    order[r] = r;
+  }
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return B->desc[a].N > B->desc[b].N; });
+  B->smem = sizeof(float4) * ((size_t)B->Nmax + 125) + sizeof(int) * (2 * (size_t)B->cellsMax + 1);
+  if (B->smem > 227 * 1024) fatal(task, "the largest replica does not fit in one block's shared memory");
+  CK(cudaMalloc(&B->dDesc, sizeof(RepDesc) * n));
+  CK(cudaMemcpy(B->dDesc, B->desc.data(), sizeof(RepDesc) * n, cudaMemcpyHostToDevice));
+  CK(cudaMalloc(&B->dOrder, sizeof(int) * n));
+  CK(cudaMemcpy(B->dOrder, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+  rep_set_smem(*B);
+  const char* e = getenv("EMDEE_REPLICA_THREADS");
+  B->threads = e ? atoi(e) : 0;
+  if (B->threads != 256 && B->threads != 512 && B->threads != 1024) B->threads = 0;
+  return B;
+}
+
+// Advances every replica by `steps` velocity-Verlet steps of dt, energies every
+// nprop steps (counted across calls), and writes each system's results back.
+void EmDee_replicas_run(void* batch, int steps, double dt, int nprop) {
+  const char* task = "replica batch run";
+  Replicas& B = *(Replicas*)batch;
+  if (steps < 0 || nprop < 1) fatal(task, "invalid number of steps");
+  for (System* s : B.sys) CK(cudaStreamSynchronize(s->stream));
+  if (B.threads == 0) B.threads = rep_autotune(B, dt, nprop);
+  if (steps == 0) return;
+  if (!B.graph || B.gSteps != steps || B.gDt != dt || B.gNprop != nprop) {
+    if (B.graph) CK(cudaGraphExecDestroy(B.graph));
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(B.stream, cudaStreamCaptureModeThreadLocal));
+    rep_launch(B, steps, dt, nprop, B.stream);
+    CK(cudaMemcpyAsync(B.hOut, B.dOut, sizeof(double) * 8 * B.n, cudaMemcpyDeviceToHost, B.stream));
+    CK(cudaStreamEndCapture(B.stream, &g));
+    CK(cudaGraphInstantiate(&B.graph, g, 0));
+    CK(cudaGraphDestroy(g));
+    B.gSteps = steps;
+    B.gDt = dt;
+    B.gNprop = nprop;
+  }
+  CK(cudaGraphLaunch(B.graph, B.stream));
+  CK(cudaStreamSynchronize(B.stream));
+  B.steps += steps;
+  const bool computeLast = B.steps % nprop == 0;
+  for (int r = 0; r < B.n; r++) {
+    const double* o = &B.hOut[8 * r];
+    if (o[6] > 0) fatal(task, "a neighbor list outgrew its capacity");
+    tEmDee* md = B.md[r];
+    System& s = *B.sys[r];
+    md->Builds += (int)o[5];
+    md->Virial.Total = o[1];
+    md->Virial.Body = 0.0;
+    if (computeLast) {
+      md->Energy.Dispersion = o[0];
+      md->Energy.Coulomb = 0.0;
+      md->Energy.Bond = 0.0;
+      md->Energy.Angle = 0.0;
+      md->Energy.Potential = o[0];
+      md->Energy.ShadowPotential = o[0];
+      for (int d = 0; d < 3; d++) {
+        md->Kinetic.TransPart[d] = 0.5 * o[2 + d];
+        md->Kinetic.RotPart[d] = 0.0;
+      }
+      md->Kinetic.Rotational = 0.0;
+      md->Kinetic.Total = md->Kinetic.TransPart[0] + md->Kinetic.TransPart[1] + md->Kinetic.TransPart[2];
+    }
+    md->Energy.UpToDate = computeLast;
+    md->Kinetic.UpToDate = computeLast;
+    // the forces belong to the current positions; the system's own lists are
+    // older than R0 now, so its next force computation rebuilds them
+    s.forcesUpToDate[0] = 1;
+    s.layerEnergy[0] = md->Energy;
+    s.layerVirial[0] = md->Virial;
+    s.r0Valid = false;
+  }
+  // device results: counters restart, the step count carries over (energies every
+  // nprop steps counted across calls)
+  std::vector<double> reset((size_t)8 * B.n, 0.0);
+  for (int r = 0; r < B.n; r++) reset[8 * r + 7] = (double)B.steps;
+  CK(cudaMemcpy(B.dOut, reset.data(), sizeof(double) * reset.size(), cudaMemcpyHostToDevice));
+}
+
+int EmDee_replicas_block_size(void* batch) { return ((Replicas*)batch)->threads; }
+
+void EmDee_replicas_destroy(void* batch) {
+  Replicas* B = (Replicas*)batch;
+  if (!B) return;
+  cudaStreamSynchronize(B->stream);
+  if (B->graph) cudaGraphExecDestroy(B->graph);
+  for (void* p : B->owned) cudaFree(p);
+  cudaFree(B->dDesc);
+  cudaFree(B->dOrder);
+  cudaFree(B->dOut);
+  cudaFreeHost(B->hOut);
+  cudaStreamDestroy(B->stream);
+  delete B;
+}
+
+}  // extern "C"

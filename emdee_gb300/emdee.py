@@ -109,12 +109,17 @@ SIGNATURES = {
     "EmDee_pair_statistics": (None, [tEmDee, _P, _P]),
     "EmDee_launch_count": (C.c_long, [tEmDee]),
     "EmDee_boost_noalloc": (C.c_int, [_P, _P, _P, _I, _D, _D, _P, _P]),
+    "EmDee_replicas_create": (C.c_void_p, [_I, _P]),
+    "EmDee_replicas_run": (None, [C.c_void_p, _I, _D, _I]),
+    "EmDee_replicas_block_size": (C.c_int, [C.c_void_p]),
+    "EmDee_replicas_destroy": (None, [C.c_void_p]),
 }
 
 # entry points of the GB300 library with no counterpart in the reference
 EXTENSIONS = {"EmDee_set_precision", "EmDee_neighbor_pairs", "EmDee_destroy", "EmDee_cuda_stream",
               "EmDee_profile", "EmDee_kernel_times", "EmDee_pair_statistics",
-              "EmDee_launch_count", "EmDee_boost_noalloc"}
+              "EmDee_launch_count", "EmDee_boost_noalloc", "EmDee_replicas_create", "EmDee_replicas_run",
+              "EmDee_replicas_block_size", "EmDee_replicas_destroy"}
 
 MIXED, FP64 = 0, 1
 

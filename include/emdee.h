@@ -261,6 +261,22 @@ int EmDee_boost_noalloc(double* P, const double* F, const double* invMass, int N
 /* Releases the system and its device memory (the reference has no destroy). */
 void EmDee_destroy(tEmDee* md);
 
+/* Replica batches (no counterpart in the reference, which runs one system per
+   call).  EmDee_replicas_create takes n initialized systems (one atom type, no
+   charges, no rigid bodies, no exclusions, one layer, mixed precision) and
+   returns a batch handle; EmDee_replicas_run advances all of them by `steps`
+   velocity-Verlet steps of dt -- the reference loop boost(dt/2), displace(dt),
+   boost(dt/2) with neighbor-list rebuilds on the skin check -- in one persistent
+   kernel launch, with energies every nprop steps (counted across calls), and
+   writes Builds, Energy, Virial and Kinetic back into each tEmDee.  The first
+   run picks the block size by timing candidates on copies of the state; every
+   (steps, dt, nprop) combination is captured once in a CUDA graph.  Systems keep
+   their device arrays: they can be downloaded, or stepped alone, between runs. */
+void* EmDee_replicas_create(int n, tEmDee** systems);
+void EmDee_replicas_run(void* batch, int steps, double dt, int nprop);
+int EmDee_replicas_block_size(void* batch);
+void EmDee_replicas_destroy(void* batch);
+
 #ifdef __cplusplus
 }
 #endif
