@@ -36,18 +36,7 @@ METRIC = "atom-steps/s"
 ORACLE_SO = os.path.join(ROOT, "oracle", "_build", "liboracle_emdee.so")
 
 
-def fcc(N, rho, jitter, seed):
-    n = 1
-    while 4 * n ** 3 < N:
-        n += 1
-    L = (N / rho) ** (1.0 / 3.0)
-    a = L / n
-    base = np.array([[0, 0, 0], [0.5, 0.5, 0], [0.5, 0, 0.5], [0, 0.5, 0.5]])
-    g = np.stack(np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij"), -1).reshape(-1, 3)
-    R = (g[:, None, :] + base[None, :, :]).reshape(-1, 3)[:N] * a
-    R += np.random.default_rng(seed).uniform(-jitter, jitter, size=R.shape)
-    return np.ascontiguousarray(R), L
-
+from emdee_gb300.workloads import KB, fcc, setup_water_box   # noqa: E402
 
 def setup(lib, W, threads=1, precision=None):
     R, L = fcc(W["N"], W["rho"], W["jitter"], W["seed"])
@@ -322,6 +311,12 @@ def run_gpu(args):
            "per_step": "EmDee_upload(momenta) from pinned host memory, boost/displace/boost, "
                        "EmDee_download(coordinates) and EmDee_download(momenta) into pinned host memory"}
 
+    # ---- the other workloads: replica batch and rigid water (throughput only) ----
+    extra = {}
+    if rank == 0 and not args.no_extra:
+        extra["lj_replicas_256"] = measure_replicas(lib, emdee_gb300, torch, args.replica_steps)
+        extra["water_rigid_4096"] = measure_water(lib, emdee_gb300, torch, args.water_steps)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         rate, threads, n, t = cpu_rate(W, budget_s=20.0, max_steps=100)
@@ -342,10 +337,76 @@ def run_gpu(args):
                                  "> 129 MB L2"},
                 "clocks": clk, "gpu_launches": int(launches), "roofline": roofline, "roofline_hbm": roofline_hbm,
                 "roofline_step": roofline_step,
-                "kernels": per_kernel, "e2e": e2e, "cpu_baseline": cpu}
+                "kernels": per_kernel, "e2e": e2e, "cpu_baseline": cpu, "workloads": extra}
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+# 256 Lennard-Jones replicas, per replica from the seed: N ~ U[256, 8192],
+# density ~ U[0.70, 0.90], T* ~ U[0.8, 2.0]; rc 2.5, skin 0.3, dt 0.005
+REPLICAS = dict(n=256, seed=86245, rc=2.5, skin=0.3, dt=0.005, nprop=100)
+
+
+def measure_replicas(lib, pkg, torch, steps):
+    rng = np.random.default_rng(REPLICAS["seed"])
+    mds, sizes = [], []
+    for k in range(REPLICAS["n"]):
+        N = int(rng.integers(256, 8193))
+        rho, T = float(rng.uniform(0.70, 0.90)), float(rng.uniform(0.8, 2.0))
+        R, L = fcc(N, rho, 0.05, REPLICAS["seed"] + k)
+        md = lib.system(1, 1, REPLICAS["rc"], REPLICAS["skin"], N)
+        lib.EmDee_set_precision(md, pkg.MIXED)
+        lib.EmDee_set_pair_model(md, 1, 1, lib.EmDee_pair_lj_cut(1.0, 1.0), 0.0)
+        lib.upload(md, "box", np.array([L]))
+        lib.upload(md, "coordinates", R)
+        lib.EmDee_random_momenta(C.byref(md), T, True, REPLICAS["seed"] + k)
+        mds.append(md)
+        sizes.append(N)
+    arr = (C.POINTER(type(mds[0])) * len(mds))(*[C.pointer(m) for m in mds])
+    b = lib.lib.EmDee_replicas_create(len(mds), C.cast(arr, C.c_void_p))
+    lib.lib.EmDee_replicas_run(b, 10, REPLICAS["dt"], REPLICAS["nprop"])   # block-size tuning + warm-up
+    builds0 = sum(m.Builds for m in mds)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    lib.lib.EmDee_replicas_run(b, steps, REPLICAS["dt"], REPLICAS["nprop"])
+    torch.cuda.synchronize()
+    t = time.perf_counter() - t0
+    total = sum(sizes)
+    out = {"metric": METRIC, "value": total * steps / t, "unit": "atom-steps/s", "replicas": len(mds),
+           "atoms": total, "N_min": min(sizes), "N_max": max(sizes), "steps": steps, "ms": 1e3 * t,
+           "block_size": lib.lib.EmDee_replicas_block_size(b),
+           "neighbor_builds": sum(m.Builds for m in mds) - builds0,
+           "timing": "host clock around one EmDee_replicas_run (one graph launch: a persistent kernel over all "
+                     "replicas, then the results read back), device synchronized on both sides",
+           "data": "synthetic (seeded fcc lattices, Maxwell-Boltzmann momenta)"}
+    lib.lib.EmDee_replicas_destroy(b)
+    for m in mds:
+        lib.lib.EmDee_destroy(C.byref(m))
+    return out
+
+
+def measure_water(lib, pkg, torch, steps):
+    """4096 rigid SPC/E molecules (12,288 atoms), coul_damped_smoothed(0.2, 1.0),
+    rc 10 A, skin 1 A, 300 K, dt 1 fs, exact rigid-body rotation, mixed precision."""
+    md = setup_water_box(lib, 4096, 86245, precision=pkg.MIXED)
+    lib.EmDee_random_momenta(C.byref(md), KB * 300.0, True, 86245)
+    W = dict(dt=1.0, nprop=100)
+    vv(lib, md, W, 5)
+    stream = torch.cuda.ExternalStream(lib.EmDee_cuda_stream(md))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    vv(lib, md, W, steps, step0=5)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    out = {"metric": METRIC, "value": 12288 * steps / (ms * 1e-3), "unit": "atom-steps/s", "atoms": 12288,
+           "steps": steps, "ms_per_step": ms / steps,
+           "timing": "CUDA events on the library stream around the velocity-Verlet loop",
+           "errors_vs_fp64_oracle": "tests/test_gpu_water_box.py (forces 1.6e-5 relative RMS, energies <= 4e-5)"}
+    lib.lib.EmDee_destroy(C.byref(md))
+    return out
 
 
 def main():
@@ -355,6 +416,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-extra", action="store_true", help="skip the replica-batch and water measurements")
+    ap.add_argument("--replica-steps", type=int, default=1000)
+    ap.add_argument("--water-steps", type=int, default=300)
     ap.add_argument("--atoms", type=int, default=None,
                     help="smaller box of the same density (profiling runs); default 1,048,576")
     args = ap.parse_args()
