@@ -252,8 +252,9 @@ void bodies_move(System& s, double CR, double CP, double dt, bool translate, boo
     CK(cudaGetLastError());
     s.prof.total++;
   }
-  k_body_move<<<body_blocks(s.nbodies), BODY_THREADS, 0, s.stream>>>(body_args(s), s.dR, CR, CP, dt, translate,
-                                                                      rotate, mode);
+  // one warp per block: the exact rotation is a long serial FP64 computation per
+  // body, so bodies are spread over as many SMs as possible
+  k_body_move<<<(s.nbodies + 31) / 32, 32, 0, s.stream>>>(body_args(s), s.dR, CR, CP, dt, translate, rotate, mode);
   CK(cudaGetLastError());
   s.prof.total++;
 }

@@ -15,8 +15,9 @@
 // and full neighbor lists (column-major, 32-bit entries: slot | stencil code).
 // Blocks are issued largest replica first.
 //
-// Scope: single atom type, no charges, no rigid bodies, no exclusions, one
-// model layer, FP32 pair arithmetic (the mixed mode).  The pair set is the
+// Scope: up to 8 atom types (pair models with their modifiers), no charges, no
+// rigid bodies, no exclusions, one model layer, FP32 pair arithmetic (the mixed
+// mode).  The pair set is the
 // reference's: FP32 prefilter, FP64 test of src/neighbor_lists.f90:247-250 for
 // candidates within 4e-5 of the threshold (this file uses -fmad=false).
 #include <algorithm>
@@ -37,7 +38,10 @@ struct RepDesc {
   int N, M, minimg, cap;
   double L, scale, skinSq, thr;   // scale = M / L; thr = (rc+skin)^2 / L^2
   float lo2, hi2, rc2, invw2, invw, Mf;
-  PairEntry<float> model;
+  PairEntry<float> model;          // type pair (1, 1)
+  int ntypes;
+  const PairEntry<float>* table;   // the system's layer-1 pair table, [jtype][itype]
+  const int* type;                 // atom types (1-based, API order)
   int* orig;        // slot -> atom
   int4* K;          // per slot: build-time unwrapped cell (x, y, z), cell rank (w)
   int4* atomK;      // per atom scratch of the same
@@ -48,6 +52,7 @@ struct RepDesc {
 };
 
 static const double REP_BAND = 4e-5;
+static const int REP_MAXT = 8;   // atom types a replica may have
 
 __device__ __forceinline__ bool rep_exact_inside(const double* R, double L, int a, int b, double thr) {
   double d[3];
@@ -99,7 +104,7 @@ struct RepShared {
 
 template <int THREADS>
 __device__ void rep_build(RepShared& S, const double* Rb, float4* pos, int* cellStart, int* cursor,
-                          const float4* offTab, bool copyR0) {
+                          const float4* offTab, bool copyR0, uint8_t* stype) {
   const RepDesc& D = S.d;
   const int N = D.N, M = D.M, cells = M * M * M;
   for (int c = threadIdx.x; c < cells; c += THREADS) cursor[c] = 0;
@@ -154,6 +159,7 @@ __device__ void rep_build(RepShared& S, const double* Rb, float4* pos, int* cell
     D.K[s] = k;
     pos[s] = make_float4((float)(Rb[3 * a] * D.scale - (double)k.x), (float)(Rb[3 * a + 1] * D.scale - (double)k.y),
                          (float)(Rb[3 * a + 2] * D.scale - (double)k.z), 0.f);
+    stype[s] = (uint8_t)(D.ntypes > 1 ? D.type[a] - 1 : 0);
   }
   __syncthreads();
   // full lists: 125 stencil cells, candidate order (z, y, x, slot)
@@ -198,8 +204,10 @@ __global__ void __launch_bounds__(THREADS) k_replicas(const RepDesc* __restrict_
   __shared__ RepShared S;
   float4* pos = (float4*)smem;
   float4* offTab = pos + Nmax;
-  int* cellStart = (int*)(offTab + 125);
+  NBParams<float>* ptab = (NBParams<float>*)(offTab + 125);   // [ti * ntypes + tj]
+  int* cellStart = (int*)(ptab + REP_MAXT * REP_MAXT);
   int* cursor = cellStart + cellsMax + 1;
+  uint8_t* stype = (uint8_t*)(cursor + cellsMax);
   if (threadIdx.x == 0) {
     S.d = descs[order[blockIdx.x]];
     S.overflow = 0;
@@ -207,12 +215,20 @@ __global__ void __launch_bounds__(THREADS) k_replicas(const RepDesc* __restrict_
   for (int c = threadIdx.x; c < 125; c += THREADS)
     offTab[c] = make_float4((float)(c % 5 - 2), (float)((c / 5) % 5 - 2), (float)(c / 25 - 2), 0.f);
   __syncthreads();
+  {
+    const int nt = S.d.ntypes;
+    for (int q = threadIdx.x; q < nt * nt; q += THREADS) {
+      const int ti = q / nt, tj = q % nt;
+      ptab[q] = S.d.table[ti * nt + tj].model;   // pair(jtype, itype) for an atom of type ti
+    }
+  }
+  __syncthreads();
   const RepDesc& D = S.d;
   const int N = D.N, lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = THREADS / 32;
   const double dt_2 = 0.5 * dt;
   int done = (int)D.out[7];
   // lists as the system's were built: from the positions of the last build (R0)
-  rep_build<THREADS>(S, D.R0, pos, cellStart, cursor, offTab, false);
+  rep_build<THREADS>(S, D.R0, pos, cellStart, cursor, offTab, false, stype);
   double builds = D.out[5];
   for (int k = 0; k < steps; k++) {
     const bool compute = (done + k + 1) % nprop == 0;
@@ -252,7 +268,7 @@ __global__ void __launch_bounds__(THREADS) k_replicas(const RepDesc* __restrict_
       __syncthreads();
     }
     if (S.rebuild) {
-      rep_build<THREADS>(S, D.R, pos, cellStart, cursor, offTab, true);
+      rep_build<THREADS>(S, D.R, pos, cellStart, cursor, offTab, true, stype);
       builds += 1.0;
     }
     // positions in cell units relative to the build-time cells
@@ -267,6 +283,7 @@ __global__ void __launch_bounds__(THREADS) k_replicas(const RepDesc* __restrict_
     float Ep = 0.f, Wp = 0.f;
     {
       const NBParams<float> mdl = D.model.model;
+      const int nt = D.ntypes;
       const float rc2 = D.rc2, invw2 = D.invw2, invw = D.invw, Mf = D.Mf;
       const bool minimg = D.minimg;
       const int cap = D.cap;
@@ -277,10 +294,12 @@ __global__ void __launch_bounds__(THREADS) k_replicas(const RepDesc* __restrict_
       for (int i = threadIdx.x; i < N; i += THREADS) {
         const float4 pi = pos[i];
         const int n = min(count[i], cap);
+        const NBParams<float>* row = ptab + (nt > 1 ? stype[i] * nt : 0);
         float fx = 0.f, fy = 0.f, fz = 0.f;
         for (int q = 0; q < n; q++) {
           const uint32_t e = __ldg(&list[(size_t)q * N + i]);
-          const float4 pj = pos[e & 0xFFFFu];
+          const int j = e & 0xFFFFu;
+          const float4 pj = pos[j];
           const float4 o = offTab[e >> 16];
           float dx = (pi.x - pj.x) - o.x, dy = (pi.y - pj.y) - o.y, dz = (pi.z - pj.z) - o.z;
           if (minimg) {
@@ -292,8 +311,14 @@ __global__ void __launch_bounds__(THREADS) k_replicas(const RepDesc* __restrict_
           const bool in = r2 < rc2;
           const float invR2c = Ops<float>::rcp(r2), invR2 = invR2c * invw2, invR = sqrtf(invR2);
           float E, W;
-          nb_compute(mdl, E, W, invR, invR2);
-          modifier_compute(mdl, E, W, invR, invR2);
+          if (nt == 1) {
+            nb_compute(mdl, E, W, invR, invR2);
+            modifier_compute(mdl, E, W, invR, invR2);
+          } else {
+            const NBParams<float>& m = row[stype[j]];
+            nb_compute(m, E, W, invR, invR2);
+            modifier_compute(m, E, W, invR, invR2);
+          }
           W = in ? W : 0.f;
           Ep += in ? E : 0.f;
           Wp += W;
@@ -472,8 +497,8 @@ void* EmDee_replicas_create(int n, tEmDee** systems) {
     tEmDee* md = systems[r];
     System& s = *sys_of(*md);
     if (!s.initialized) fatal(task, "every system must be initialized (box and coordinates uploaded)");
-    if (s.ntypes != 1 || s.nbodies > 0 || s.hasExclusions || s.nlayers != 1 || s.precision != 0)
-      fatal(task, "replicas must have one atom type, no bodies, no exclusions, one layer and mixed precision");
+    if (s.ntypes > REP_MAXT || s.nbodies > 0 || s.hasExclusions || s.nlayers != 1 || s.precision != 0)
+      fatal(task, "replicas must have at most 8 atom types, no bodies, no exclusions, one layer and mixed precision");
     for (int a = 0; a < s.natoms; a++)
       if (s.charged[a]) fatal(task, "replicas must carry no charges");
     if (s.natoms > 65535) fatal(task, "replicas are limited to 65535 atoms");
@@ -503,6 +528,9 @@ void* EmDee_replicas_create(int n, tEmDee** systems) {
     d.invw = (float)(1.0 / w);
     d.Mf = (float)d.M;
     CK(cudaMemcpy(&d.model, s.models.d32, sizeof(PairEntry<float>), cudaMemcpyDeviceToHost));
+    d.ntypes = s.ntypes;
+    d.table = s.models.d32;
+    d.type = s.dType;
     // list capacity: twice the ideal-gas count within rc+skin, at least 64
     const double expect = 4.0 / 3.0 * 3.14159265358979 * std::pow(s.xRc, 3) * s.natoms / (L * L * L);
     d.cap = std::max(64, ((int)(2.0 * expect) + 7) / 8 * 8);
@@ -521,7 +549,8 @@ void* EmDee_replicas_create(int n, tEmDee** systems) {
     order[r] = r;
   }
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return B->desc[a].N > B->desc[b].N; });
-  B->smem = sizeof(float4) * ((size_t)B->Nmax + 125) + sizeof(int) * (2 * (size_t)B->cellsMax + 1);
+  B->smem = sizeof(float4) * ((size_t)B->Nmax + 125) + sizeof(NBParams<float>) * REP_MAXT * REP_MAXT +
+            sizeof(int) * (2 * (size_t)B->cellsMax + 1) + (size_t)B->Nmax;
   if (B->smem > 227 * 1024) fatal(task, "the largest replica does not fit in one block's shared memory");
   CK(cudaMalloc(&B->dDesc, sizeof(RepDesc) * n));
   CK(cudaMemcpy(B->dDesc, B->desc.data(), sizeof(RepDesc) * n, cudaMemcpyHostToDevice));

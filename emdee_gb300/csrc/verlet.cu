@@ -172,6 +172,10 @@ static void ensure(double*& p, size_t& cap, size_t need) {
 }
 
 static int vv_blocks(int n) { return n > 0 ? (n + VV_THREADS - 1) / VV_THREADS : 1; }
+// body kernels run one warp per block: their per-body work is long and serial (FP64
+// rotations), so bodies are spread over as many SMs as possible
+static const int VV_BODY_THREADS = 32;
+static int vv_body_blocks(int n) { return n > 0 ? (n + VV_BODY_THREADS - 1) / VV_BODY_THREADS : 1; }
 
 void device_verlet_pre(System& s, double dt, bool compute, int mode) {
   VerletScratch& w = s.verlet;
@@ -194,11 +198,11 @@ void device_verlet_pre(System& s, double dt, bool compute, int mode) {
     ensure(w.r0, w.r0Cap, (size_t)3 * s.nbodies);
     ensure(w.q0, w.q0Cap, (size_t)4 * s.nbodies);
     if (compute)
-      k_vv_pre_body<true><<<vv_blocks(s.nbodies), VV_THREADS, 0, s.stream>>>(body_args(s), s.F(), s.dR, dt, dt_2,
-                                                                             mode, w.r0, w.q0);
+      k_vv_pre_body<true><<<vv_body_blocks(s.nbodies), VV_BODY_THREADS, 0, s.stream>>>(body_args(s), s.F(), s.dR, dt,
+                                                                                        dt_2, mode, w.r0, w.q0);
     else
-      k_vv_pre_body<false><<<vv_blocks(s.nbodies), VV_THREADS, 0, s.stream>>>(body_args(s), s.F(), s.dR, dt, dt_2,
-                                                                              mode, w.r0, w.q0);
+      k_vv_pre_body<false><<<vv_body_blocks(s.nbodies), VV_BODY_THREADS, 0, s.stream>>>(body_args(s), s.F(), s.dR, dt,
+                                                                                         dt_2, mode, w.r0, w.q0);
     CK(cudaGetLastError());
     s.prof.total++;
   }
@@ -213,14 +217,14 @@ void device_verlet_post(System& s, double dt, bool compute, int mode, double* ou
   const int nf = all ? s.natoms : s.nfree;
   double vb[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, vf[5] = {0, 0, 0, 0, 0};
   if (s.nbodies > 0) {
-    const int blocks = vv_blocks(s.nbodies);
+    const int blocks = vv_body_blocks(s.nbodies);
     ensure(w.partB, w.partBCap, (size_t)9 * blocks);
     if (compute)
-      k_vv_post_body<true><<<blocks, VV_THREADS, 0, s.stream>>>(body_args(s), s.F(), dt, dt_2, mode, w.r0, w.q0,
-                                                                w.partB, s.dTicket + 5, s.dResult + 24);
+      k_vv_post_body<true><<<blocks, VV_BODY_THREADS, 0, s.stream>>>(body_args(s), s.F(), dt, dt_2, mode, w.r0, w.q0,
+                                                                     w.partB, s.dTicket + 5, s.dResult + 24);
     else
-      k_vv_post_body<false><<<blocks, VV_THREADS, 0, s.stream>>>(body_args(s), s.F(), dt, dt_2, mode, w.r0, w.q0,
-                                                                 nullptr, nullptr, nullptr);
+      k_vv_post_body<false><<<blocks, VV_BODY_THREADS, 0, s.stream>>>(body_args(s), s.F(), dt, dt_2, mode, w.r0,
+                                                                      w.q0, nullptr, nullptr, nullptr);
     CK(cudaGetLastError());
     s.prof.total++;
   }

@@ -103,3 +103,35 @@ def test_single_system_continues_after_batch(gpu, oracle):
     velocity_verlet(oracle, ref, DT, STEPS, NPROP)
     assert abs(md.Energy.Potential - ref.Energy.Potential) < 1e-4 * abs(ref.Energy.Potential)
     assert np.abs(gpu.download(md, "coordinates", (N, 3)) - oracle.download(ref, "coordinates", (N, 3))).max() < 1e-4
+
+
+def make_binary(lib, N, k, precision=None):
+    """80:20 Lennard-Jones mixture (eps_AB 1.5, sigma_AB 0.8, eps_BB 0.5, sigma_BB 0.88), rho 1.2, T* 0.8."""
+    R, L = fcc(N, 1.2, 0.05, SEED + k)
+    types = np.where(np.random.default_rng(SEED + k).random(N) < 0.8, 1, 2)
+    md = lib.system(1, 1, 2.5, 0.3, N, types, [1.0, 1.0])
+    if precision is not None:
+        lib.EmDee_set_precision(md, precision)
+    lib.EmDee_set_pair_model(md, 1, 1, lib.EmDee_pair_lj_cut(1.0, 1.0), 0.0)
+    lib.EmDee_set_pair_model(md, 2, 2, lib.EmDee_pair_lj_cut(0.5, 0.88), 0.0)
+    lib.EmDee_set_pair_model(md, 1, 2, lib.EmDee_pair_lj_cut(1.5, 0.8), 0.0)
+    lib.upload(md, "box", np.array([L]))
+    lib.upload(md, "coordinates", R)
+    lib.EmDee_random_momenta(C.byref(md), 0.8, True, SEED + k)
+    return md
+
+
+def test_replicas_binary_mixture(gpu, oracle):
+    sizes = [864, 500, 1372]
+    mds = [make_binary(gpu, N, k, MIXED) for k, N in enumerate(sizes)]
+    b, keep = batch(gpu, mds)
+    gpu.lib.EmDee_replicas_run(b, STEPS, 0.004, NPROP)
+    for k, N in enumerate(sizes):
+        got = state(gpu, mds[k], N)
+        ref_md = make_binary(oracle, N, k)
+        velocity_verlet(oracle, ref_md, 0.004, STEPS, NPROP)
+        ref = state(oracle, ref_md, N)
+        rel = np.abs(got[0] - ref[0]) / np.abs(ref[0])
+        print(N, "binary batch vs oracle", rel, np.abs(got[2] - ref[2]).max(), got[1], ref[1])
+        assert rel.max() < 1e-4 and np.abs(got[2] - ref[2]).max() < 1e-4 and got[1] == ref[1]
+    gpu.lib.EmDee_replicas_destroy(b)
