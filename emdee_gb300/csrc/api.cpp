@@ -1104,6 +1104,18 @@ void EmDee_compute_forces(tEmDee* md) {
   compute_forces_impl(md);
 }
 
+// Device address of the system's coordinates, momenta or forces (double[N][3], API order),
+// for zero-copy use by other CUDA code on the library's stream.  Writes through it bypass
+// the library's bookkeeping: upload the array afterwards, or use it only through calls
+// that treat it as input (the replica batches).
+void* EmDee_device_pointer(tEmDee md, const char* item) {
+  System& s = *sys_of(md);
+  if (!strcmp(item, "coordinates")) return s.dR;
+  if (!strcmp(item, "momenta")) return s.dP;
+  if (!strcmp(item, "forces")) return s.F();
+  fatal("device pointer", "unknown item");
+}
+
 // src/EmDeeCode.f90:1107-1211
 void EmDee_verlet_step(tEmDee* md, double dt) {
   System& s = *sys_of(*md);

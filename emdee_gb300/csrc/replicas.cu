@@ -230,8 +230,12 @@ __global__ void __launch_bounds__(THREADS) k_replicas(const RepDesc* __restrict_
   // lists as the system's were built: from the positions of the last build (R0)
   rep_build<THREADS>(S, D.R0, pos, cellStart, cursor, offTab, false, stype);
   double builds = D.out[5];
-  for (int k = 0; k < steps; k++) {
-    const bool compute = (done + k + 1) % nprop == 0;
+  // steps < 0: forces, energy and virial at the current positions only
+  const bool evaluate = steps < 0;
+  const int nsteps = evaluate ? 1 : steps;
+  for (int k = 0; k < nsteps; k++) {
+    const bool compute = evaluate || (k + 1) % nprop == 0;   // every nprop-th step of this call
+    if (!evaluate) {
     // boost(dt/2) and displace(dt), FP64 (src/EmDeeData.f90:823-896)
     for (int a = threadIdx.x; a < N; a += THREADS) {
       const double im = D.unitMass ? 1.0 : D.invMass[a];
@@ -271,6 +275,7 @@ __global__ void __launch_bounds__(THREADS) k_replicas(const RepDesc* __restrict_
       rep_build<THREADS>(S, D.R, pos, cellStart, cursor, offTab, true, stype);
       builds += 1.0;
     }
+    }   // !evaluate
     // positions in cell units relative to the build-time cells
     for (int s = threadIdx.x; s < N; s += THREADS) {
       const int a = D.orig[s];
@@ -347,6 +352,7 @@ __global__ void __launch_bounds__(THREADS) k_replicas(const RepDesc* __restrict_
       for (int w = 0; w < nw; w++) ff_add(h, l, S.wff[threadIdx.x][w].x, S.wff[threadIdx.x][w].y);
       if (threadIdx.x == 1 || compute) D.out[threadIdx.x] = (double)h + (double)l;
     }
+    if (evaluate) break;
     // boost(dt/2) with the new forces; kinetic energies on compute steps
     double ke[3] = {0.0, 0.0, 0.0};
     for (int a = threadIdx.x; a < N; a += THREADS) {
@@ -374,7 +380,7 @@ __global__ void __launch_bounds__(THREADS) k_replicas(const RepDesc* __restrict_
   if (threadIdx.x == 0) {
     D.out[5] = builds;
     D.out[6] = (double)S.overflow;
-    D.out[7] = (double)(done + steps);
+    D.out[7] = (double)(done + (evaluate ? 0 : steps));
   }
 }
 
@@ -396,6 +402,8 @@ struct Replicas {
   int gSteps = -1, gNprop = -1;
   double gDt = 0.0;
   int steps = 0;
+  std::vector<double*> saved;     // checkpoints: R, F, R0 per replica
+  std::vector<tEmDee> savedMd;
 };
 
 static void rep_launch(Replicas& B, int steps, double dt, int nprop, cudaStream_t st) {
@@ -563,8 +571,8 @@ void* EmDee_replicas_create(int n, tEmDee** systems) {
   return B;
 }
 
-// Advances every replica by `steps` velocity-Verlet steps of dt, energies every
-// nprop steps (counted across calls), and writes each system's results back.
+// Advances every replica by `steps` velocity-Verlet steps of dt, energies at every
+// nprop-th step of the call, and writes each system's results back.
 void EmDee_replicas_run(void* batch, int steps, double dt, int nprop) {
   const char* task = "replica batch run";
   Replicas& B = *(Replicas*)batch;
@@ -588,7 +596,7 @@ void EmDee_replicas_run(void* batch, int steps, double dt, int nprop) {
   CK(cudaGraphLaunch(B.graph, B.stream));
   CK(cudaStreamSynchronize(B.stream));
   B.steps += steps;
-  const bool computeLast = B.steps % nprop == 0;
+  const bool computeLast = steps % nprop == 0;
   for (int r = 0; r < B.n; r++) {
     const double* o = &B.hOut[8 * r];
     if (o[6] > 0) fatal(task, "a neighbor list outgrew its capacity");
@@ -620,8 +628,7 @@ void EmDee_replicas_run(void* batch, int steps, double dt, int nprop) {
     s.layerVirial[0] = md->Virial;
     s.r0Valid = false;
   }
-  // device results: counters restart, the step count carries over (energies every
-  // nprop steps counted across calls)
+  // device results: counters restart; the device keeps the total step count
   std::vector<double> reset((size_t)8 * B.n, 0.0);
   for (int r = 0; r < B.n; r++) reset[8 * r + 7] = (double)B.steps;
   CK(cudaMemcpy(B.dOut, reset.data(), sizeof(double) * reset.size(), cudaMemcpyHostToDevice));
@@ -629,12 +636,118 @@ void EmDee_replicas_run(void* batch, int steps, double dt, int nprop) {
 
 int EmDee_replicas_block_size(void* batch) { return ((Replicas*)batch)->threads; }
 
+// Forces, potential energy and virial of every replica at its current positions (lists
+// rebuilt from them, which then become the build positions R0); no step is taken and no
+// build is counted.  Energy and Virial are written back into each tEmDee.
+void EmDee_replicas_evaluate(void* batch) {
+  Replicas& B = *(Replicas*)batch;
+  for (System* s : B.sys) CK(cudaStreamSynchronize(s->stream));
+  if (B.threads == 0) B.threads = 1024;
+  for (int r = 0; r < B.n; r++)
+    CK(cudaMemcpyAsync(B.desc[r].R0, B.desc[r].R, sizeof(double) * 3 * B.desc[r].N, cudaMemcpyDeviceToDevice,
+                       B.stream));
+  rep_launch(B, -1, 0.0, 1, B.stream);
+  CK(cudaMemcpyAsync(B.hOut, B.dOut, sizeof(double) * 8 * B.n, cudaMemcpyDeviceToHost, B.stream));
+  CK(cudaStreamSynchronize(B.stream));
+  for (int r = 0; r < B.n; r++) {
+    const double* o = &B.hOut[8 * r];
+    if (o[6] > 0) fatal("replica batch evaluation", "a neighbor list outgrew its capacity");
+    tEmDee* md = B.md[r];
+    md->Energy.Dispersion = o[0];
+    md->Energy.Coulomb = md->Energy.Bond = md->Energy.Angle = 0.0;
+    md->Energy.Potential = md->Energy.ShadowPotential = o[0];
+    md->Energy.UpToDate = true;
+    md->Virial.Total = o[1];
+    md->Virial.Body = 0.0;
+    System& s = *B.sys[r];
+    s.forcesUpToDate[0] = 1;
+    s.layerEnergy[0] = md->Energy;
+    s.layerVirial[0] = md->Virial;
+    s.r0Valid = false;
+  }
+  std::vector<double> reset((size_t)8 * B.n, 0.0);
+  for (int r = 0; r < B.n; r++) reset[8 * r + 7] = (double)B.steps;
+  CK(cudaMemcpy(B.dOut, reset.data(), sizeof(double) * reset.size(), cudaMemcpyHostToDevice));
+}
+
+// Copies item ("coordinates", "momenta" or "forces") of every replica into / from one
+// contiguous device array [n][N][3] (replicas of equal size), on the batch stream.
+static double* rep_item(RepDesc& d, const char* item) {
+  if (!strcmp(item, "coordinates")) return d.R;
+  if (!strcmp(item, "momenta")) return d.P;
+  if (!strcmp(item, "forces")) return d.F;
+  fatal("replica batch copy", "unknown item");
+}
+
+void EmDee_replicas_gather(void* batch, const char* item, double* dst) {
+  Replicas& B = *(Replicas*)batch;
+  size_t off = 0;
+  for (int r = 0; r < B.n; r++) {
+    const size_t n = (size_t)3 * B.desc[r].N;
+    CK(cudaMemcpyAsync(dst + off, rep_item(B.desc[r], item), sizeof(double) * n, cudaMemcpyDeviceToDevice, B.stream));
+    off += n;
+  }
+  CK(cudaStreamSynchronize(B.stream));
+}
+
+void EmDee_replicas_scatter(void* batch, const char* item, const double* src) {
+  Replicas& B = *(Replicas*)batch;
+  size_t off = 0;
+  for (int r = 0; r < B.n; r++) {
+    const size_t n = (size_t)3 * B.desc[r].N;
+    CK(cudaMemcpyAsync(rep_item(B.desc[r], item), src + off, sizeof(double) * n, cudaMemcpyDeviceToDevice, B.stream));
+    off += n;
+  }
+  CK(cudaStreamSynchronize(B.stream));
+}
+
+// Saves (R, F, R0, Energy, Virial) of every replica; EmDee_replicas_restore puts them back for
+// the replicas whose mask entry is nonzero (Metropolis rejections in hybrid Monte Carlo)
+void EmDee_replicas_checkpoint(void* batch) {
+  Replicas& B = *(Replicas*)batch;
+  if (B.saved.empty()) {
+    for (int r = 0; r < B.n; r++) {
+      double* p;
+      CK(cudaMalloc(&p, sizeof(double) * 9 * B.desc[r].N));
+      B.saved.push_back(p);
+    }
+    B.savedMd.resize(B.n);
+  }
+  for (int r = 0; r < B.n; r++) {
+    const size_t b3 = sizeof(double) * 3 * B.desc[r].N;
+    CK(cudaMemcpyAsync(B.saved[r], B.desc[r].R, b3, cudaMemcpyDeviceToDevice, B.stream));
+    CK(cudaMemcpyAsync(B.saved[r] + 3 * B.desc[r].N, B.desc[r].F, b3, cudaMemcpyDeviceToDevice, B.stream));
+    CK(cudaMemcpyAsync(B.saved[r] + 6 * B.desc[r].N, B.desc[r].R0, b3, cudaMemcpyDeviceToDevice, B.stream));
+    B.savedMd[r] = *B.md[r];
+  }
+  CK(cudaStreamSynchronize(B.stream));
+}
+
+void EmDee_replicas_restore(void* batch, const int* mask) {
+  Replicas& B = *(Replicas*)batch;
+  if (B.saved.empty()) fatal("replica batch restore", "no checkpoint has been taken");
+  for (int r = 0; r < B.n; r++) {
+    if (!mask[r]) continue;
+    const size_t b3 = sizeof(double) * 3 * B.desc[r].N;
+    CK(cudaMemcpyAsync(B.desc[r].R, B.saved[r], b3, cudaMemcpyDeviceToDevice, B.stream));
+    CK(cudaMemcpyAsync(B.desc[r].F, B.saved[r] + 3 * B.desc[r].N, b3, cudaMemcpyDeviceToDevice, B.stream));
+    CK(cudaMemcpyAsync(B.desc[r].R0, B.saved[r] + 6 * B.desc[r].N, b3, cudaMemcpyDeviceToDevice, B.stream));
+    tEmDee* md = B.md[r];
+    const int builds = md->Builds;
+    md->Energy = B.savedMd[r].Energy;
+    md->Virial = B.savedMd[r].Virial;
+    md->Builds = builds;
+  }
+  CK(cudaStreamSynchronize(B.stream));
+}
+
 void EmDee_replicas_destroy(void* batch) {
   Replicas* B = (Replicas*)batch;
   if (!B) return;
   cudaStreamSynchronize(B->stream);
   if (B->graph) cudaGraphExecDestroy(B->graph);
   for (void* p : B->owned) cudaFree(p);
+  for (double* p : B->saved) cudaFree(p);
   cudaFree(B->dDesc);
   cudaFree(B->dOrder);
   cudaFree(B->dOut);

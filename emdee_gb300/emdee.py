@@ -113,13 +113,36 @@ SIGNATURES = {
     "EmDee_replicas_run": (None, [C.c_void_p, _I, _D, _I]),
     "EmDee_replicas_block_size": (C.c_int, [C.c_void_p]),
     "EmDee_replicas_destroy": (None, [C.c_void_p]),
+    "EmDee_replicas_evaluate": (None, [C.c_void_p]),
+    "EmDee_replicas_checkpoint": (None, [C.c_void_p]),
+    "EmDee_replicas_restore": (None, [C.c_void_p, _P]),
+    "EmDee_replicas_gather": (None, [C.c_void_p, C.c_char_p, _P]),
+    "EmDee_replicas_scatter": (None, [C.c_void_p, C.c_char_p, _P]),
+    "EmDee_device_pointer": (C.c_void_p, [tEmDee, C.c_char_p]),
+    "EmDee_surrogate_param_count": (_I, []),
+    "EmDee_surrogate_create": (C.c_void_p, [_I, _I, _D, _P, _D, _D, _D, _D, _D]),
+    "EmDee_surrogate_set_params": (None, [C.c_void_p, _P]),
+    "EmDee_surrogate_get_params": (None, [C.c_void_p, _P]),
+    "EmDee_surrogate_descriptors": (None, [C.c_void_p, _P, _P, _I, _P]),
+    "EmDee_surrogate_forces": (_I, [C.c_void_p, _P, _P, _P, _I, _P]),
+    "EmDee_surrogate_atom_outputs": (None, [C.c_void_p, _P, _P, _P]),
+    "EmDee_surrogate_gradient": (None, [C.c_void_p, _P, _P, _P, _D, _D, _P, _P, _P]),
+    "EmDee_surrogate_adam": (None, [C.c_void_p, _P, _D, _I, _P]),
+    "EmDee_surrogate_trajectory": (None, [C.c_void_p, _P, _P, _P, _P, _I, _D, _P]),
+    "EmDee_surrogate_destroy": (None, [C.c_void_p]),
 }
 
 # entry points of the GB300 library with no counterpart in the reference
 EXTENSIONS = {"EmDee_set_precision", "EmDee_neighbor_pairs", "EmDee_destroy", "EmDee_cuda_stream",
               "EmDee_profile", "EmDee_kernel_times", "EmDee_pair_statistics",
               "EmDee_launch_count", "EmDee_boost_noalloc", "EmDee_replicas_create", "EmDee_replicas_run",
-              "EmDee_replicas_block_size", "EmDee_replicas_destroy"}
+              "EmDee_replicas_block_size", "EmDee_replicas_destroy", "EmDee_replicas_evaluate",
+              "EmDee_replicas_checkpoint", "EmDee_replicas_restore", "EmDee_device_pointer",
+              "EmDee_replicas_gather", "EmDee_replicas_scatter",
+              "EmDee_surrogate_param_count", "EmDee_surrogate_create", "EmDee_surrogate_set_params",
+              "EmDee_surrogate_get_params", "EmDee_surrogate_descriptors", "EmDee_surrogate_forces",
+              "EmDee_surrogate_atom_outputs", "EmDee_surrogate_gradient", "EmDee_surrogate_adam",
+              "EmDee_surrogate_trajectory", "EmDee_surrogate_destroy"}
 
 MIXED, FP64 = 0, 1
 

@@ -267,7 +267,7 @@ void EmDee_destroy(tEmDee* md);
    returns a batch handle; EmDee_replicas_run advances all of them by `steps`
    velocity-Verlet steps of dt -- the reference loop boost(dt/2), displace(dt),
    boost(dt/2) with neighbor-list rebuilds on the skin check -- in one persistent
-   kernel launch, with energies every nprop steps (counted across calls), and
+   kernel launch, with energies at every nprop-th step of the call, and
    writes Builds, Energy, Virial and Kinetic back into each tEmDee.  The first
    run picks the block size by timing candidates on copies of the state; every
    (steps, dt, nprop) combination is captured once in a CUDA graph.  Systems keep
@@ -276,6 +276,42 @@ void* EmDee_replicas_create(int n, tEmDee** systems);
 void EmDee_replicas_run(void* batch, int steps, double dt, int nprop);
 int EmDee_replicas_block_size(void* batch);
 void EmDee_replicas_destroy(void* batch);
+/* Forces, potential energy and virial of every replica at its current positions (no step). */
+void EmDee_replicas_evaluate(void* batch);
+/* Save positions, forces and energies of every replica; restore those with mask[r] != 0
+   (the rejections of hybrid Monte Carlo). */
+void EmDee_replicas_checkpoint(void* batch);
+void EmDee_replicas_restore(void* batch, const int* mask);
+/* Copy "coordinates", "momenta" or "forces" of all replicas to / from one contiguous device
+   array [n][N][3]. */
+void EmDee_replicas_gather(void* batch, const char* item, double* dst);
+void EmDee_replicas_scatter(void* batch, const char* item, const double* src);
+
+/* Device address (double[N][3], API order) of "coordinates", "momenta" or "forces", for
+   zero-copy access from other CUDA code (no reference counterpart: the reference keeps its
+   arrays in host memory, see EmDee_memory_address). */
+void* EmDee_device_pointer(tEmDee md, const char* item);
+
+/* Learned surrogate potential for hybrid Monte Carlo proposals (no reference counterpart):
+   per-atom radial descriptors (16 Gaussians x 2 species, smooth cut-off), one
+   32-64-64-1 SiLU network per species evaluated on the BF16 tensor cores, forces by the
+   adjoint of the descriptors, energy+force training with Adam.  Device arrays are FP64
+   [chains][N][3] positions/forces and [chains] energies; parameters are FP32, packed per
+   species as W1[32][64], b1[64], W2[64][64], b2[64], w3[64], b3. */
+int EmDee_surrogate_param_count(void);
+void* EmDee_surrogate_create(int chains, int N, double L, const int* types, double rc, double skin, double mu0,
+                             double mu15, double width);
+void EmDee_surrogate_set_params(void* s, const float* params);
+void EmDee_surrogate_get_params(void* s, float* params);
+void EmDee_surrogate_descriptors(void* s, const double* dR, float* dG, int rebuild, void* stream);
+int EmDee_surrogate_forces(void* s, const double* dR, double* dF, double* dE, int rebuild, void* stream);
+void EmDee_surrogate_atom_outputs(void* s, float* dEatom, float* dEdG, void* stream);
+void EmDee_surrogate_gradient(void* s, const double* dR, const double* dEtrue, const double* dFtrue, double wE,
+                              double wF, float* dGrad, double* loss, void* stream);
+void EmDee_surrogate_adam(void* s, const float* dGrad, double lr, int step, void* stream);
+void EmDee_surrogate_trajectory(void* s, double* dR, double* dP, double* dF, double* dE, int n, double dt,
+                                void* stream);
+void EmDee_surrogate_destroy(void* s);
 
 #ifdef __cplusplus
 }
