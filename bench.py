@@ -267,12 +267,15 @@ def run_gpu(args):
                 "peak_source": "cuBLAS SGEMM 8192^3, TF32 off, measured in this run",
                 "flops_per_launch": flops, "half_list_pairs": listed.value, "pairs_within_rc": within.value,
                 "us_per_launch": pair_s * 1e6}
-    boost_bytes = 72.0 * N   # P read+write, F read
-    move_bytes = 80.0 * N    # R read+write, P read, 1/m read
+    boost_bytes = 72.0 * N   # P read+write, F read (steps with energies only)
+    # fused step (two deferred kicks + move + skin displacement + FP32 packing), unit masses:
+    # P r/w 48, F 24, R r/w 48, R0 24, build-time cell 16, slot 4, charge 8, packed position 16
+    move_bytes = 188.0 * N
     hbm = peaks.get("hbm_gbs", 6800.0)
     boost_gbs = boost_bytes / (kms[4] / kn[4] * 1e-3) / 1e9 if kn[4] else None
     move_gbs = move_bytes / (kms[5] / kn[5] * 1e-3) / 1e9 if kn[5] else None
-    roofline_hbm = {"bound": "hbm", "kernel": "k_move (EmDee_displace)", "achieved": move_gbs, "peak": hbm,
+    roofline_hbm = {"bound": "hbm", "kernel": "k_step_fused (EmDee_displace: deferred boosts, move, skin, pack)",
+                    "achieved": move_gbs, "peak": hbm,
                     "unit": "GB/s", "frac": (move_gbs / hbm) if move_gbs else None, "traffic": None,
                     "peak_source": peak_kind, "boost_achieved_gbs": boost_gbs}
 

@@ -200,6 +200,7 @@ static void mark_stale(System& s, tEmDee* md) {
     s.layerEnergy[l].UpToDate = false;
   }
   md->Energy.UpToDate = false;
+  s.skinReady = s.packReady = false;
 }
 
 // ---- host mirrors of EmDee_memory_address ---------------------------------------
@@ -283,8 +284,9 @@ static void compute_forces_impl(tEmDee* md) {
   if (!s.initialized) fatal("compute forces", "system has not been initialized");
   bool compute = md->Options.Compute;
   double t0 = wtime();
+  flush_pending(s);   // deferred boosts use the forces they were issued with
   bool rebuild = !s.r0Valid;
-  if (!rebuild) rebuild = device_skin_check(s);
+  if (!rebuild) rebuild = s.skinReady ? device_skin_from_step(s) : device_skin_check(s);
   else s.hResult[9] = 1.0;
   if (rebuild) {
     device_build_lists(s);
@@ -292,7 +294,9 @@ static void compute_forces_impl(tEmDee* md) {
   }
   double t1 = wtime();
   md->Time.Neighbor += t1 - t0;
-  device_pack(s);
+  // the build packs the FP32 positions for its prefilter; a fused step packs them too
+  if (!((rebuild || s.packReady) && s.precision == 0)) device_pack(s);
+  s.skinReady = s.packReady = false;
   device_pair_forces(s, compute);
   const double* r = s.hResult;   // Epair, Ecoul, Wpair, Wcoul
   double Elong = 0.0, Wlong = 0.0;
@@ -755,6 +759,8 @@ void EmDee_upload(tEmDee* md, char* option, double* address) {
   System& s = *sys_of(*md);
   char item[257];
   option_string(option, item);
+  if (!strcmp(item, "momenta")) sys_of(*md)->npend = 0;   // replaced: pending kicks are moot
+  else flush_pending(*sys_of(*md));
   if (!address) fatal("upload", "provided address is invalid");
   size_t n3 = (size_t)3 * s.natoms;
   MirrorScope scope(s);
@@ -821,6 +827,7 @@ void EmDee_upload(tEmDee* md, char* option, double* address) {
 
 // src/EmDeeCode.f90:659-801 (free-atom options)
 void EmDee_download(tEmDee md, char* option, double* address) {
+  flush_pending(*sys_of(md));
   System& s = *sys_of(md);
   char item[257];
   option_string(option, item);
@@ -887,6 +894,7 @@ void EmDee_download(tEmDee md, char* option, double* address) {
 // it ends, so the caller may read and write it between calls.
 void* EmDee_memory_address(tEmDee md, char* option) {
   System& s = *sys_of(md);
+  flush_pending(s);
   char item[257];
   option_string(option, item);
   size_t b = sizeof(double) * 3 * s.natoms;
@@ -914,6 +922,9 @@ void* EmDee_memory_address(tEmDee md, char* option) {
 void EmDee_share_phase_space(tEmDee mdkeep, tEmDee* mdlose) {
   const char* task = "phase space sharing";
   System &keep = *sys_of(mdkeep), &lose = *sys_of(*mdlose);
+  flush_pending(keep);
+  flush_pending(lose);
+  keep.phaseShared = lose.phaseShared = true;
   if (!(keep.initialized && lose.initialized)) fatal(task, "EmDee system 1 has not been initialized");
   if (keep.natoms != lose.natoms) fatal(task, "different numbers of atoms");
   for (int i = 0; i < keep.natoms; i++) {
@@ -954,6 +965,7 @@ void EmDee_share_phase_space(tEmDee mdkeep, tEmDee* mdlose) {
 // src/EmDeeCode.f90:929-946
 void EmDee_switch_model_layer(tEmDee* md, int layer) {
   System& s = *sys_of(*md);
+  flush_pending(s);   // pending kicks belong to the current layer's forces
   if (layer != s.layer) {
     if (layer < 1 || layer > s.nlayers) fatal("model layer switch", "selected layer is out of range");
     s.layer = layer;
@@ -965,6 +977,7 @@ void EmDee_switch_model_layer(tEmDee* md, int layer) {
 // src/EmDeeCode.f90:950-1020 (serial KISS/ziggurat draws on the host, as the reference)
 void EmDee_random_momenta(tEmDee* md, double kT, bool adjust, int seed) {
   System& s = *sys_of(*md);
+  s.npend = 0;   // the momenta are replaced
   MirrorScope scope(s);
   int N = s.natoms;
   std::vector<double> P((size_t)3 * N, 0.0);
@@ -1061,6 +1074,17 @@ void EmDee_boost(tEmDee* md, double lambda, double alpha, double dt) {
   bool compute = md->Options.Compute;
   if (lambda != 0.0 && !s.forcesUpToDate[s.layer - 1]) compute_forces_impl(md);
   bool translate = md->Options.Translate, rotate = md->Options.Rotate;
+  // Without energies, a plain kick (CP = 1, free atoms) is deferred to the next
+  // kernel that touches P: the fused step of EmDee_displace, or a flush.  The
+  // arithmetic and its order are unchanged.
+  if (!compute && CP == 1.0 && s.nbodies == 0 && translate && !scope.active && s.initialized && !s.phaseShared &&
+      s.forcesUpToDate[s.layer - 1]) {
+    if (s.npend == 2) flush_pending(s);
+    s.pendCF[s.npend++] = CF;
+    md->Kinetic.UpToDate = false;
+    return;
+  }
+  flush_pending(s);
   if (s.nbodies > 0) bodies_boost(s, CP, CF, translate, rotate, compute);
   else if (translate) device_boost(s, CP, CF, compute);
   if (compute) {
@@ -1090,9 +1114,16 @@ void EmDee_displace(tEmDee* md, double lambda, double alpha, double dt) {
     CR = 1.0;
   }
   CP = lambda * CP;
-  if (s.nbodies > 0) bodies_move(s, CR, CP, dt, md->Options.Translate, md->Options.Rotate, md->Options.RotationMode);
-  else if (md->Options.Translate) device_move(s, CR, CP);
-  mark_stale(s, md);
+  if (s.nbodies == 0 && md->Options.Translate && CR == 1.0 && s.initialized) {
+    // pending boosts, the move, the skin displacement and the FP32 packing in one pass
+    mark_stale(s, md);
+    device_step_fused(s, CP);
+  } else {
+    flush_pending(s);
+    if (s.nbodies > 0) bodies_move(s, CR, CP, dt, md->Options.Translate, md->Options.Rotate, md->Options.RotationMode);
+    else if (md->Options.Translate) device_move(s, CR, CP);
+    mark_stale(s, md);
+  }
   md->Time.Motion += wtime() - t0;
 }
 
@@ -1110,6 +1141,7 @@ void EmDee_compute_forces(tEmDee* md) {
 // that treat it as input (the replica batches).
 void* EmDee_device_pointer(tEmDee md, const char* item) {
   System& s = *sys_of(md);
+  flush_pending(s);
   if (!strcmp(item, "coordinates")) return s.dR;
   if (!strcmp(item, "momenta")) return s.dP;
   if (!strcmp(item, "forces")) return s.F();
@@ -1121,6 +1153,8 @@ void EmDee_verlet_step(tEmDee* md, double dt) {
   System& s = *sys_of(*md);
   MirrorScope scope(s);
   if (!s.initialized) fatal("verlet step", "system has not been initialized");
+  flush_pending(s);
+  s.skinReady = s.packReady = false;
   const bool compute = md->Options.Compute;
   const int mode = md->Options.RotationMode;
   double t0 = wtime();

@@ -20,8 +20,10 @@ static const int MOTION_THREADS = 256;
 
 // UNITCP: CP == 1, so CP*P == P exactly and is skipped; UNITM: all masses are
 // 1, so multiplications by 1/m are skipped.  Both leave every rounding as in
-// the reference's statements.
-template <bool KIN, bool UNITCP, bool UNITM>
+// the reference's statements.  FMA (mixed precision only): the update is one
+// fused multiply-add, which halves the work on GB300's narrow FP64 pipe; FP64
+// mode keeps the reference's separately rounded statements.
+template <bool KIN, bool UNITCP, bool UNITM, bool FMA>
 __global__ void __launch_bounds__(MOTION_THREADS) k_boost(double* __restrict__ P, const double* __restrict__ F,
                                                           const double* __restrict__ invMass, int N, double CP,
                                                           double CF, double* partials, unsigned int* ticket,
@@ -30,7 +32,8 @@ __global__ void __launch_bounds__(MOTION_THREADS) k_boost(double* __restrict__ P
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
     double im = (KIN && !UNITM) ? invMass[i] : 1.0;
     for (int d = 0; d < 3; d++) {
-      double p = (UNITCP ? P[3 * i + d] : CP * P[3 * i + d]) + CF * F[3 * i + d];
+      const double base = UNITCP ? P[3 * i + d] : CP * P[3 * i + d];
+      double p = FMA ? fma(CF, F[3 * i + d], base) : base + CF * F[3 * i + d];
       P[3 * i + d] = p;
       if (KIN) k2[d] += UNITM ? p * p : im * (p * p);
     }
@@ -38,7 +41,7 @@ __global__ void __launch_bounds__(MOTION_THREADS) k_boost(double* __restrict__ P
   if (KIN) grid_reduce<3, MOTION_THREADS>(k2, partials, ticket, result + 10);
 }
 
-template <bool UNITCR, bool UNITM>
+template <bool UNITCR, bool UNITM, bool FMA>
 __global__ void __launch_bounds__(MOTION_THREADS) k_move(double* __restrict__ R, const double* __restrict__ P,
                                                          const double* __restrict__ invMass, int N, double CR,
                                                          double CP) {
@@ -46,8 +49,9 @@ __global__ void __launch_bounds__(MOTION_THREADS) k_move(double* __restrict__ R,
   if (i >= N) return;
   double im = UNITM ? 1.0 : invMass[i];
   for (int d = 0; d < 3; d++) {
-    double dr = UNITM ? CP * P[3 * i + d] : CP * P[3 * i + d] * im;
-    R[3 * i + d] = (UNITCR ? R[3 * i + d] : CR * R[3 * i + d]) + dr;
+    const double base = UNITCR ? R[3 * i + d] : CR * R[3 * i + d];
+    if (FMA) R[3 * i + d] = UNITM ? fma(CP, P[3 * i + d], base) : fma(CP * P[3 * i + d], im, base);
+    else R[3 * i + d] = base + (UNITM ? CP * P[3 * i + d] : CP * P[3 * i + d] * im);
   }
 }
 
@@ -56,7 +60,8 @@ static int motion_blocks(int N) {
   return b < 1184 ? b : 1184;   // 152 SMs x 8 resident blocks, grid-stride beyond
 }
 
-void device_boost(System& s, double CP, double CF, bool kinetic) {
+template <bool FMA>
+static void boost_launch(System& s, double CP, double CF, bool kinetic) {
   int N = s.natoms, blocks = motion_blocks(N);
   if (kinetic) {
     if (s.keCap < blocks) {
@@ -65,8 +70,8 @@ void device_boost(System& s, double CP, double CF, bool kinetic) {
       CK(cudaMalloc(&s.dKE, sizeof(double) * 3 * blocks));
     }
     prof_begin(s, PK_BOOST);
-    auto kern = CP == 1.0 ? (s.unitMass ? k_boost<true, true, true> : k_boost<true, true, false>)
-                          : (s.unitMass ? k_boost<true, false, true> : k_boost<true, false, false>);
+    auto kern = CP == 1.0 ? (s.unitMass ? k_boost<true, true, true, FMA> : k_boost<true, true, false, FMA>)
+                          : (s.unitMass ? k_boost<true, false, true, FMA> : k_boost<true, false, false, FMA>);
     kern<<<blocks, MOTION_THREADS, 0, s.stream>>>(s.dP, s.F(), s.dInvMass, N, CP, CF, s.dKE, s.dTicket + 1,
                                                   s.dResult);
     CK(cudaGetLastError());
@@ -75,21 +80,37 @@ void device_boost(System& s, double CP, double CF, bool kinetic) {
     CK(cudaStreamSynchronize(s.stream));
   } else {
     prof_begin(s, PK_BOOST);
-    auto kern = CP == 1.0 ? k_boost<false, true, true> : k_boost<false, false, true>;
+    auto kern = CP == 1.0 ? k_boost<false, true, true, FMA> : k_boost<false, false, true, FMA>;
     kern<<<blocks, MOTION_THREADS, 0, s.stream>>>(s.dP, s.F(), s.dInvMass, N, CP, CF, nullptr, nullptr, nullptr);
     CK(cudaGetLastError());
     prof_end(s, PK_BOOST);
   }
 }
 
-void device_move(System& s, double CR, double CP) {
+void device_boost(System& s, double CP, double CF, bool kinetic) {
+  if (s.precision == 0) boost_launch<true>(s, CP, CF, kinetic);
+  else boost_launch<false>(s, CP, CF, kinetic);
+}
+
+template <bool FMA>
+static void move_launch(System& s, double CR, double CP) {
   int N = s.natoms;
   prof_begin(s, PK_MOVE);
-  auto kern = CR == 1.0 ? (s.unitMass ? k_move<true, true> : k_move<true, false>)
-                        : (s.unitMass ? k_move<false, true> : k_move<false, false>);
+  auto kern = CR == 1.0 ? (s.unitMass ? k_move<true, true, FMA> : k_move<true, false, FMA>)
+                        : (s.unitMass ? k_move<false, true, FMA> : k_move<false, false, FMA>);
   kern<<<(N + MOTION_THREADS - 1) / MOTION_THREADS, MOTION_THREADS, 0, s.stream>>>(s.dR, s.dP, s.dInvMass, N, CR, CP);
   CK(cudaGetLastError());
   prof_end(s, PK_MOVE);
+}
+
+void device_move(System& s, double CR, double CP) {
+  if (s.precision == 0) move_launch<true>(s, CR, CP);
+  else move_launch<false>(s, CR, CP);
+}
+
+void flush_pending(System& s) {
+  for (int k = 0; k < s.npend; k++) device_boost(s, 1.0, s.pendCF[k], false);
+  s.npend = 0;
 }
 
 // Chooses the force kernel for the current layer and leaves the four sums in
@@ -217,8 +238,8 @@ extern "C" int EmDee_boost_noalloc(double* P, const double* F, const double* inv
   cudaError_t e = cudaMemsetAsync(ticket, 0, sizeof(unsigned int), st);
   int blocks = motion_blocks(N);
   bool unitCP = CP == 1.0, unitM = invMass == nullptr;
-  auto kern = unitCP ? (unitM ? k_boost<true, true, true> : k_boost<true, true, false>)
-                     : (unitM ? k_boost<true, false, true> : k_boost<true, false, false>);
+  auto kern = unitCP ? (unitM ? k_boost<true, true, true, false> : k_boost<true, true, false, false>)
+                     : (unitM ? k_boost<true, false, true, false> : k_boost<true, false, false, false>);
   if (e == cudaSuccess) {
     kern<<<blocks, MOTION_THREADS, 0, st>>>(P, F, invMass, N, CP, CF, scratch, ticket, twoKE - 10);
     e = cudaGetLastError();

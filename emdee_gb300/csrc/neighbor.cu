@@ -143,12 +143,15 @@ bool device_skin_check(System& s) {
 // binning (src/neighbor_lists.f90:122-128) and tile sort
 // ---------------------------------------------------------------------------------
 
-__global__ void k_assign(const double* __restrict__ R, int N, double L, TileGeom g, int4* atomK, int* count) {
+__global__ void k_assign(const double* __restrict__ R, int N, double invL, TileGeom g, int4* atomK, double* atomKd,
+                         int* count) {
   int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= N) return;
   int c[3], K[3];
   for (int d = 0; d < 3; d++) {
-    double rs = R[3 * a + d] / L, fl = floor(rs);
+    // R * (1/L): a cell index that differs from the reference's R / L by an ulp at a
+    // cell boundary changes only the order of candidates, not the pair set
+    double rs = R[3 * a + d] * invL, fl = floor(rs);
     int ci = (int)(g.M * (rs - fl));
     ci = ci < 0 ? 0 : (ci >= g.M ? g.M - 1 : ci);   // M*(x - floor x) may round up to M
     c[d] = ci;
@@ -156,6 +159,7 @@ __global__ void k_assign(const double* __restrict__ R, int N, double L, TileGeom
   }
   int rank = cell_rank(g, c[0], c[1], c[2]);
   atomK[a] = make_int4(K[0], K[1], K[2], rank);
+  for (int d = 0; d < 3; d++) atomKd[3 * a + d] = (double)K[d];
   atomicAdd(&count[rank], 1);
 }
 
@@ -229,11 +233,13 @@ __global__ void k_sort_cells(const int* start, int nRanks, int* orig) {
   }
 }
 
-__global__ void k_fill_slots(const int* orig, int N, const int4* atomK, const int* type, int4* K, uint8_t* type8) {
+__global__ void k_fill_slots(const int* orig, int N, const int4* atomK, const int* type, int4* K, uint8_t* type8,
+                             int* slotOf) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= N) return;
   int a = orig[s];
   K[s] = atomK[a];
+  slotOf[a] = s;
   type8[s] = (uint8_t)(type[a] - 1);
 }
 
@@ -508,6 +514,10 @@ void device_build_lists(System& s) {
       CK(cudaFree(g.dOrig)); CK(cudaFree(g.dK)); CK(cudaFree(g.dAtomK)); CK(cudaFree(g.dPos4));
       CK(cudaFree(g.dType8)); CK(cudaFree(g.dRs64)); CK(cudaFree(g.dNbCount)); CK(cudaFree(g.dNbInner));
       CK(cudaFree(g.dSelf));
+      CK(cudaFree(g.dSlotOf));
+      CK(cudaFree(g.dAtomKd));
+      CK(cudaMalloc(&g.dSlotOf, sizeof(int) * N));
+      CK(cudaMalloc(&g.dAtomKd, sizeof(double) * 3 * N));
       CK(cudaMalloc(&g.dOrig, sizeof(int) * N));
       CK(cudaMalloc(&g.dK, sizeof(int4) * N));
       CK(cudaMalloc(&g.dAtomK, sizeof(int4) * N));
@@ -528,12 +538,12 @@ void device_build_lists(System& s) {
     CK(cudaMemsetAsync(g.dCount, 0, sizeof(int) * (g.nRanks + 1), s.stream));
     CK(cudaMemsetAsync(g.dCursor, 0, sizeof(int) * (g.nRanks + 1), s.stream));
     s.prof.total += 8;   // assign, 3 scan phases, scatter, sort, fill, tile info
-    k_assign<<<bl, th, 0, s.stream>>>(s.dR, N, L, geo, g.dAtomK, g.dCount);
+    k_assign<<<bl, th, 0, s.stream>>>(s.dR, N, 1.0 / L, geo, g.dAtomK, g.dAtomKd, g.dCount);
     CK(cudaGetLastError());
     device_scan(s, g.dCount, g.dStart, g.nRanks);
     k_scatter<<<bl, th, 0, s.stream>>>(g.dAtomK, N, g.dStart, g.dCursor, g.dOrig);
     k_sort_cells<<<(g.nRanks + 255) / 256, 256, 0, s.stream>>>(g.dStart, g.nRanks, g.dOrig);
-    k_fill_slots<<<bl, th, 0, s.stream>>>(g.dOrig, N, g.dAtomK, s.dType, g.dK, g.dType8);
+    k_fill_slots<<<bl, th, 0, s.stream>>>(g.dOrig, N, g.dAtomK, s.dType, g.dK, g.dType8, g.dSlotOf);
     int* dMax = g.dTileInfo + 2 * g.nTiles;
     CK(cudaMemsetAsync(dMax, 0, sizeof(int) * 4, s.stream));
     k_tile_info<<<g.nTiles, 128, 0, s.stream>>>(g.dStart, geo, g.dTileInfo, dMax);
@@ -824,6 +834,141 @@ void device_rdf_counts(System& s, int bins, double Rc, const std::vector<uint8_t
   CK(cudaFree(dHas));
   CK(cudaFree(dOn));
   CK(cudaFree(dHist));
+}
+
+// ---------------------------------------------------------------------------------
+// fused step: pending boosts, move, skin displacement and FP32 packing in one pass
+// ---------------------------------------------------------------------------------
+
+// Contiguous atom ranges combined in index order, as in k_skin, so the skin value
+// is the same for any range size.  Each
+// statement rounds as the separate kernels do (this file uses -fmad=false).
+static const int STEP_CHUNKS = 2;   // 64 consecutive atoms per warp: many warps in flight
+
+// FMA (mixed precision only): the updates use fused multiply-adds, which halves the
+// work on the FP64 pipe (the limit of this kernel on GB300); FP64 mode keeps the
+// reference's separately rounded statements.
+template <int NK, bool UNITM, bool PACK, bool FMA>
+__global__ void __launch_bounds__(SKIN_THREADS) k_step_fused(double* __restrict__ R, double* __restrict__ P,
+                                                             const double* __restrict__ F,
+                                                             const double* __restrict__ invMass,
+                                                             const double* __restrict__ R0, int N, double cf0,
+                                                             double cf1, double CP, double skinSq,
+                                                             const int* __restrict__ slotOf,
+                                                             const double* __restrict__ atomKd,
+                                                             const double* __restrict__ charge, double scale,
+                                                             float4* __restrict__ pos4, longlong2* partial,
+                                                             unsigned int* ticket, double* result) {
+  __shared__ MaxPrev wsum[SKIN_THREADS / 32];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int base = (blockIdx.x * (SKIN_THREADS / 32) + warp) * 32 * STEP_CHUNKS;
+  MaxPrev run{-1, -1};
+  for (int c = 0; c < STEP_CHUNKS; c++) {
+    const int i = base + c * 32 + lane;
+    MaxPrev v{-1, -1};
+    if (i < N) {
+      const double im = UNITM ? 1.0 : invMass[i];
+      double r[3];
+      for (int d = 0; d < 3; d++) {
+        double p = P[3 * i + d];
+        if (FMA) {
+          if (NK >= 1) p = fma(cf0, F[3 * i + d], p);
+          if (NK >= 2) p = fma(cf1, F[3 * i + d], p);
+        } else {
+          if (NK >= 1) p = p + cf0 * F[3 * i + d];
+          if (NK >= 2) p = p + cf1 * F[3 * i + d];
+        }
+        if (NK >= 1) P[3 * i + d] = p;
+        if (FMA) r[d] = UNITM ? fma(CP, p, R[3 * i + d]) : fma(CP * p, im, R[3 * i + d]);
+        else r[d] = R[3 * i + d] + (UNITM ? CP * p : CP * p * im);
+        R[3 * i + d] = r[d];
+      }
+      const double d0 = r[0] - R0[3 * i], d1 = r[1] - R0[3 * i + 1], d2 = r[2] - R0[3 * i + 2];
+      v.m = __double_as_longlong(FMA ? fma(d2, d2, fma(d1, d1, d0 * d0)) : d0 * d0 + d1 * d1 + d2 * d2);
+      if (PACK) {
+        const double q = charge[i];
+        float u[3];
+        for (int d = 0; d < 3; d++)
+          u[d] = (float)(FMA ? fma(r[d], scale, -atomKd[3 * i + d]) : r[d] * scale - atomKd[3 * i + d]);
+        pos4[slotOf[i]] = make_float4(u[0], u[1], u[2], fabs(q) > 2.220446049250313e-16 ? (float)q : 0.0f);
+      }
+    }
+    v = warp_ordered_combine(v);
+    run = mp_combine(run, v);
+  }
+  if (lane == 0) wsum[warp] = run;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    MaxPrev b = wsum[0];
+    for (int w = 1; w < SKIN_THREADS / 32; w++) b = mp_combine(b, wsum[w]);
+    partial[blockIdx.x] = make_longlong2(b.m, b.p);
+    __threadfence();
+    last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  const int nb = gridDim.x, per = (nb + SKIN_THREADS - 1) / SKIN_THREADS;
+  MaxPrev acc{-1, -1};
+  for (int k = 0; k < per; k++) {
+    int b = threadIdx.x * per + k;
+    if (b < nb) {
+      longlong2 v = __ldcg(&partial[b]);
+      acc = mp_combine(acc, MaxPrev{v.x, v.y});
+    }
+  }
+  acc = warp_ordered_combine(acc);
+  if (lane == 0) wsum[warp] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    MaxPrev b = wsum[0];
+    for (int w = 1; w < SKIN_THREADS / 32; w++) b = mp_combine(b, wsum[w]);
+    double maximum = __longlong_as_double(b.m), next = __longlong_as_double(b.p < 0 ? b.m : b.p);
+    double value = maximum + 2 * sqrt(maximum * next) + next;
+    result[8] = value;
+    result[9] = value > skinSq ? 1.0 : 0.0;
+    *ticket = 0;
+  }
+}
+
+void device_step_fused(System& s, double CP) {
+  const int N = s.natoms;
+  const int blocks = (N + SKIN_THREADS * STEP_CHUNKS - 1) / (SKIN_THREADS * STEP_CHUNKS);
+  ensure_partials(s, blocks);
+  const bool pack = s.precision == 0 && s.r0Valid;
+  const Grid& g = s.grid;
+  const double scale = g.M > 0 ? (double)g.M / *s.Lbox : 0.0;
+  prof_begin(s, PK_MOVE);
+#define STEP_ARGS s.dR, s.dP, s.F(), s.dInvMass, s.dR0, N, s.pendCF[0], s.pendCF[1], CP, s.skinSq, g.dSlotOf, \
+                  g.dAtomKd, s.dCharge, scale, g.dPos4, (longlong2*)s.dPartials, s.dTicket, s.dResult
+#define STEP_LAUNCH(NK, UM, PK, FM) k_step_fused<NK, UM, PK, FM><<<blocks, SKIN_THREADS, 0, s.stream>>>(STEP_ARGS)
+#define STEP_NK(UM, PK, FM)                 \
+  if (s.npend == 0) STEP_LAUNCH(0, UM, PK, FM); \
+  else if (s.npend == 1) STEP_LAUNCH(1, UM, PK, FM); \
+  else STEP_LAUNCH(2, UM, PK, FM);
+  if (pack) {   // mixed precision: fused multiply-adds
+    if (s.unitMass) { STEP_NK(true, true, true) } else { STEP_NK(false, true, true) }
+  } else if (s.precision == 0) {
+    if (s.unitMass) { STEP_NK(true, false, true) } else { STEP_NK(false, false, true) }
+  } else {
+    if (s.unitMass) { STEP_NK(true, false, false) } else { STEP_NK(false, false, false) }
+  }
+#undef STEP_NK
+#undef STEP_LAUNCH
+#undef STEP_ARGS
+  CK(cudaGetLastError());
+  prof_end(s, PK_MOVE);
+  s.npend = 0;
+  s.skinReady = s.r0Valid;
+  s.packReady = pack;
+}
+
+// the skin value left by the fused step
+bool device_skin_from_step(System& s) {
+  CK(cudaMemcpyAsync(s.hResult + 8, s.dResult + 8, 2 * sizeof(double), cudaMemcpyDeviceToHost, s.stream));
+  CK(cudaStreamSynchronize(s.stream));
+  return s.hResult[9] != 0.0;
 }
 
 }  // namespace emdee

@@ -510,6 +510,7 @@ void* EmDee_replicas_create(int n, tEmDee** systems) {
     for (int a = 0; a < s.natoms; a++)
       if (s.charged[a]) fatal(task, "replicas must carry no charges");
     if (s.natoms > 65535) fatal(task, "replicas are limited to 65535 atoms");
+    flush_pending(s);
     CK(cudaStreamSynchronize(s.stream));
     RepDesc d;
     memset(&d, 0, sizeof d);
@@ -577,7 +578,10 @@ void EmDee_replicas_run(void* batch, int steps, double dt, int nprop) {
   const char* task = "replica batch run";
   Replicas& B = *(Replicas*)batch;
   if (steps < 0 || nprop < 1) fatal(task, "invalid number of steps");
-  for (System* s : B.sys) CK(cudaStreamSynchronize(s->stream));
+  for (System* s : B.sys) {
+    flush_pending(*s);
+    CK(cudaStreamSynchronize(s->stream));
+  }
   if (B.threads == 0) B.threads = rep_autotune(B, dt, nprop);
   if (steps == 0) return;
   if (!B.graph || B.gSteps != steps || B.gDt != dt || B.gNprop != nprop) {
@@ -641,7 +645,10 @@ int EmDee_replicas_block_size(void* batch) { return ((Replicas*)batch)->threads;
 // build is counted.  Energy and Virial are written back into each tEmDee.
 void EmDee_replicas_evaluate(void* batch) {
   Replicas& B = *(Replicas*)batch;
-  for (System* s : B.sys) CK(cudaStreamSynchronize(s->stream));
+  for (System* s : B.sys) {
+    flush_pending(*s);
+    CK(cudaStreamSynchronize(s->stream));
+  }
   if (B.threads == 0) B.threads = 1024;
   for (int r = 0; r < B.n; r++)
     CK(cudaMemcpyAsync(B.desc[r].R0, B.desc[r].R, sizeof(double) * 3 * B.desc[r].N, cudaMemcpyDeviceToDevice,
@@ -681,6 +688,7 @@ static double* rep_item(RepDesc& d, const char* item) {
 
 void EmDee_replicas_gather(void* batch, const char* item, double* dst) {
   Replicas& B = *(Replicas*)batch;
+  for (System* sy : B.sys) flush_pending(*sy);
   size_t off = 0;
   for (int r = 0; r < B.n; r++) {
     const size_t n = (size_t)3 * B.desc[r].N;
@@ -692,6 +700,7 @@ void EmDee_replicas_gather(void* batch, const char* item, double* dst) {
 
 void EmDee_replicas_scatter(void* batch, const char* item, const double* src) {
   Replicas& B = *(Replicas*)batch;
+  for (System* sy : B.sys) flush_pending(*sy);
   size_t off = 0;
   for (int r = 0; r < B.n; r++) {
     const size_t n = (size_t)3 * B.desc[r].N;
@@ -705,6 +714,7 @@ void EmDee_replicas_scatter(void* batch, const char* item, const double* src) {
 // the replicas whose mask entry is nonzero (Metropolis rejections in hybrid Monte Carlo)
 void EmDee_replicas_checkpoint(void* batch) {
   Replicas& B = *(Replicas*)batch;
+  for (System* sy : B.sys) flush_pending(*sy);
   if (B.saved.empty()) {
     for (int r = 0; r < B.n; r++) {
       double* p;

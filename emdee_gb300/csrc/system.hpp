@@ -119,6 +119,8 @@ struct Grid {
   uint16_t* dSelf = nullptr;   // halo index of each slot in its own tile
   int4* dK = nullptr;
   int4* dAtomK = nullptr;
+  int* dSlotOf = nullptr;   // atom -> slot of the last build
+  double* dAtomKd = nullptr;   // the build-time unwrapped cell of each atom, as doubles
   float4* dPos4 = nullptr;
   uint8_t* dType8 = nullptr;
   double* dRs64 = nullptr;
@@ -201,6 +203,13 @@ struct System {
   DevModels models;
   bool modelsUploaded = false;
   bool r0Valid = false;        // R0 holds the positions of the last build
+  // deferred boosts (P += CF F with CP = 1 and no energies), applied by the next kernel
+  // that touches P; the fused move also leaves the skin-check value and the packed
+  // FP32 positions of the new coordinates (valid until R or the lists change)
+  int npend = 0;
+  double pendCF[2] = {0.0, 0.0};
+  bool skinReady = false, packReady = false;
+  bool phaseShared = false;   // R/P aliased with another system (no deferral then)
   double builtL = 0;           // box length at the last build
 
   // reduction scratch
@@ -249,6 +258,11 @@ void device_pair_forces(System& s, bool compute);
 void device_boost(System& s, double CP, double CF, bool kinetic);
 // R <- CR R + CP P / m (free atoms).
 void device_move(System& s, double CR, double CP);
+// pending boosts + move (CR = 1) + skin displacement + FP32 packing in one pass
+void device_step_fused(System& s, double CP);
+// applies pending boosts (before anything reads P or replaces F)
+void flush_pending(System& s);
+bool device_skin_from_step(System& s);
 void device_pair_statistics(System& s, long* listed, long* within);
 // Rigid bodies (bodies.cu).
 void bodies_update(System& s);

@@ -20,7 +20,7 @@ namespace emdee {
 static const int VV_THREADS = 128;
 
 // list == nullptr: atoms 0..n-1; otherwise the atoms list[0..n-1]
-template <bool COMPUTE>
+template <bool COMPUTE, bool FMA>
 __global__ void __launch_bounds__(VV_THREADS) k_vv_pre_free(double* __restrict__ R, double* __restrict__ P,
                                                             const double* __restrict__ F,
                                                             const double* __restrict__ invMass, const int* list,
@@ -32,14 +32,15 @@ __global__ void __launch_bounds__(VV_THREADS) k_vv_pre_free(double* __restrict__
   for (int d = 0; d < 3; d++) {
     const double p = P[3 * j + d], f = F[3 * j + d];
     if (COMPUTE) s0[3 * q + d] = 2.5 * R[3 * j + d] + dt_2 * im * (p - dt_2 * f);
-    const double pn = 1.0 * p + dt_2 * f;
+    const double pn = FMA ? fma(dt_2, f, p) : 1.0 * p + dt_2 * f;
     P[3 * j + d] = pn;
-    R[3 * j + d] = 1.0 * R[3 * j + d] + dt * pn * im;
+    R[3 * j + d] = FMA ? (list == nullptr && im == 1.0 ? fma(dt, pn, R[3 * j + d]) : fma(dt * pn, im, R[3 * j + d]))
+                       : 1.0 * R[3 * j + d] + dt * pn * im;
   }
 }
 
 // v[0..2] 2KE_t per dimension, v[3] Ks_t, v[4] Us
-template <bool COMPUTE>
+template <bool COMPUTE, bool FMA>
 __global__ void __launch_bounds__(VV_THREADS) k_vv_post_free(const double* __restrict__ R, double* __restrict__ P,
                                                              const double* __restrict__ F,
                                                              const double* __restrict__ invMass, const int* list,
@@ -53,7 +54,7 @@ __global__ void __launch_bounds__(VV_THREADS) k_vv_post_free(const double* __res
     double p[3], f[3];
     for (int d = 0; d < 3; d++) {
       f[d] = F[3 * j + d];
-      p[d] = 1.0 * P[3 * j + d] + dt_2 * f[d];
+      p[d] = FMA ? fma(dt_2, f[d], P[3 * j + d]) : 1.0 * P[3 * j + d] + dt_2 * f[d];
       P[3 * j + d] = p[d];
     }
     if (COMPUTE) {
@@ -177,7 +178,8 @@ static int vv_blocks(int n) { return n > 0 ? (n + VV_THREADS - 1) / VV_THREADS :
 static const int VV_BODY_THREADS = 32;
 static int vv_body_blocks(int n) { return n > 0 ? (n + VV_BODY_THREADS - 1) / VV_BODY_THREADS : 1; }
 
-void device_verlet_pre(System& s, double dt, bool compute, int mode) {
+template <bool FMA>
+static void verlet_pre(System& s, double dt, bool compute, int mode) {
   VerletScratch& w = s.verlet;
   const double dt_2 = 0.5 * dt;
   const bool all = s.nbodies == 0;
@@ -186,10 +188,10 @@ void device_verlet_pre(System& s, double dt, bool compute, int mode) {
   if (nf > 0) {
     const int* list = all ? nullptr : s.dFree;
     if (compute)
-      k_vv_pre_free<true><<<vv_blocks(nf), VV_THREADS, 0, s.stream>>>(s.dR, s.dP, s.F(), s.dInvMass, list, nf, dt,
+      k_vv_pre_free<true, FMA><<<vv_blocks(nf), VV_THREADS, 0, s.stream>>>(s.dR, s.dP, s.F(), s.dInvMass, list, nf, dt,
                                                                       dt_2, w.s0);
     else
-      k_vv_pre_free<false><<<vv_blocks(nf), VV_THREADS, 0, s.stream>>>(s.dR, s.dP, s.F(), s.dInvMass, list, nf, dt,
+      k_vv_pre_free<false, FMA><<<vv_blocks(nf), VV_THREADS, 0, s.stream>>>(s.dR, s.dP, s.F(), s.dInvMass, list, nf, dt,
                                                                        dt_2, w.s0);
     CK(cudaGetLastError());
     s.prof.total++;
@@ -210,7 +212,8 @@ void device_verlet_pre(System& s, double dt, bool compute, int mode) {
 
 // out[0..2] 2KE_t, [3..5] 2KE_r, [6] Ks_t, [7] Ks_r, [8] Us (bodies first, then free atoms,
 // as each thread of the reference sums them)
-void device_verlet_post(System& s, double dt, bool compute, int mode, double* out) {
+template <bool FMA>
+static void verlet_post(System& s, double dt, bool compute, int mode, double* out) {
   VerletScratch& w = s.verlet;
   const double dt_2 = 0.5 * dt;
   const bool all = s.nbodies == 0;
@@ -233,10 +236,10 @@ void device_verlet_post(System& s, double dt, bool compute, int mode, double* ou
     ensure(w.partF, w.partFCap, (size_t)5 * blocks);
     const int* list = all ? nullptr : s.dFree;
     if (compute)
-      k_vv_post_free<true><<<blocks, VV_THREADS, 0, s.stream>>>(s.dR, s.dP, s.F(), s.dInvMass, list, nf, dt, dt_2,
+      k_vv_post_free<true, FMA><<<blocks, VV_THREADS, 0, s.stream>>>(s.dR, s.dP, s.F(), s.dInvMass, list, nf, dt, dt_2,
                                                                 w.s0, w.partF, s.dTicket + 6, s.dResult + 34);
     else
-      k_vv_post_free<false><<<blocks, VV_THREADS, 0, s.stream>>>(s.dR, s.dP, s.F(), s.dInvMass, list, nf, dt, dt_2,
+      k_vv_post_free<false, FMA><<<blocks, VV_THREADS, 0, s.stream>>>(s.dR, s.dP, s.F(), s.dInvMass, list, nf, dt, dt_2,
                                                                  w.s0, nullptr, nullptr, nullptr);
     CK(cudaGetLastError());
     s.prof.total++;
@@ -253,6 +256,16 @@ void device_verlet_post(System& s, double dt, bool compute, int mode, double* ou
   out[6] = vb[6] + vf[3];
   out[7] = vb[7];
   out[8] = vb[8] + vf[4];
+}
+
+void device_verlet_pre(System& s, double dt, bool compute, int mode) {
+  if (s.precision == 0) verlet_pre<true>(s, dt, compute, mode);
+  else verlet_pre<false>(s, dt, compute, mode);
+}
+
+void device_verlet_post(System& s, double dt, bool compute, int mode, double* out) {
+  if (s.precision == 0) verlet_post<true>(s, dt, compute, mode, out);
+  else verlet_post<false>(s, dt, compute, mode, out);
 }
 
 }  // namespace emdee
