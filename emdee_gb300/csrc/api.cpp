@@ -563,9 +563,10 @@ void EmDee_destroy(tEmDee* md) {
   cudaFree(s->dExCount);
   cudaFree(s->dExItem);
   Grid& g = s->grid;
-  cudaFree(g.dCount); cudaFree(g.dStart); cudaFree(g.dCursor); cudaFree(g.dScanTmp); cudaFree(g.dOrig);
+  cudaFree(g.dCount); cudaFree(g.dStart); cudaFree(g.dScanTmp); cudaFree(g.dOrig);
   cudaFree(g.dSelf); cudaFree(g.dK); cudaFree(g.dAtomK); cudaFree(g.dPos4); cudaFree(g.dType8);
   cudaFree(g.dRs64); cudaFree(g.dNb); cudaFree(g.dHaloTab); cudaFree(g.dNbCount); cudaFree(g.dNbInner); cudaFree(g.dTileInfo);
+  cudaFree(g.dSlotOf); cudaFree(g.dAtomKd); cudaFree(g.dKeyX);
   cudaFree(s->models.d64); cudaFree(s->models.d32); cudaFree(s->models.coul64); cudaFree(s->models.coul32);
   cudaFree(s->models.interact);
   cudaFree(s->dPartials);
@@ -787,8 +788,12 @@ void EmDee_upload(tEmDee* md, char* option, double* address) {
     CK(cudaMemcpyAsync(s.dP, address, sizeof(double) * n3, cudaMemcpyHostToDevice, s.stream));
     if (s.hMirrorP) memcpy(s.hMirrorP, address, sizeof(double) * n3);
     double t2[3] = {0, 0, 0}, r2[3] = {0, 0, 0};   // src/EmDeeData.f90:157-189
-    for (int i : s.freeList)
-      for (int d = 0; d < 3; d++) t2[d] += s.invMass[i] * (address[3 * i + d] * address[3 * i + d]);
+    if (s.nbodies == 0) {
+      device_kinetic(s, t2);   // every atom is free: sum on the device
+    } else {
+      for (int i : s.freeList)
+        for (int d = 0; d < 3; d++) t2[d] += s.invMass[i] * (address[3 * i + d] * address[3 * i + d]);
+    }
     if (s.nbodies > 0) {
       double k6[6];
       bodies_assign(s, k6);

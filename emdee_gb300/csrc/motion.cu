@@ -60,6 +60,23 @@ static int motion_blocks(int N) {
   return b < 1184 ? b : 1184;   // 152 SMs x 8 resident blocks, grid-stride beyond
 }
 
+// 2KE per dimension = sum over atoms of P^2/m (src/EmDeeData.f90:157-189, free
+// atoms), into result[10..12]
+template <bool UNITM>
+__global__ void __launch_bounds__(MOTION_THREADS) k_kinetic(const double* __restrict__ P,
+                                                            const double* __restrict__ invMass, int N,
+                                                            double* partials, unsigned int* ticket, double* result) {
+  double k2[3] = {0.0, 0.0, 0.0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    const double im = UNITM ? 1.0 : invMass[i];
+    for (int d = 0; d < 3; d++) {
+      const double p = P[3 * i + d];
+      k2[d] += UNITM ? p * p : im * (p * p);
+    }
+  }
+  grid_reduce<3, MOTION_THREADS>(k2, partials, ticket, result + 10);
+}
+
 template <bool FMA>
 static void boost_launch(System& s, double CP, double CF, bool kinetic) {
   int N = s.natoms, blocks = motion_blocks(N);
@@ -106,6 +123,21 @@ static void move_launch(System& s, double CR, double CP) {
 void device_move(System& s, double CR, double CP) {
   if (s.precision == 0) move_launch<true>(s, CR, CP);
   else move_launch<false>(s, CR, CP);
+}
+
+void device_kinetic(System& s, double* twoKE) {
+  int N = s.natoms, blocks = motion_blocks(N);
+  if (s.keCap < blocks) {
+    CK(cudaFree(s.dKE));
+    s.keCap = blocks;
+    CK(cudaMalloc(&s.dKE, sizeof(double) * 3 * blocks));
+  }
+  auto kern = s.unitMass ? k_kinetic<true> : k_kinetic<false>;
+  kern<<<blocks, MOTION_THREADS, 0, s.stream>>>(s.dP, s.dInvMass, N, s.dKE, s.dTicket + 1, s.dResult);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(s.hResult + 10, s.dResult + 10, 3 * sizeof(double), cudaMemcpyDeviceToHost, s.stream));
+  CK(cudaStreamSynchronize(s.stream));
+  for (int d = 0; d < 3; d++) twoKE[d] = s.hResult[10 + d];
 }
 
 void flush_pending(System& s) {

@@ -144,7 +144,7 @@ bool device_skin_check(System& s) {
 // ---------------------------------------------------------------------------------
 
 __global__ void k_assign(const double* __restrict__ R, int N, double invL, TileGeom g, int4* atomK, double* atomKd,
-                         int* count) {
+                         int* count, int* inCell) {
   int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= N) return;
   int c[3], K[3];
@@ -160,7 +160,15 @@ __global__ void k_assign(const double* __restrict__ R, int N, double invL, TileG
   int rank = cell_rank(g, c[0], c[1], c[2]);
   atomK[a] = make_int4(K[0], K[1], K[2], rank);
   for (int d = 0; d < 3; d++) atomKd[3 * a + d] = (double)K[d];
-  atomicAdd(&count[rank], 1);
+  // one atomic per distinct cell of the warp (neighbouring atoms often share a
+  // cell); each atom keeps its place among the cell's atoms for the scatter
+  const unsigned active = __activemask();
+  const unsigned peers = __match_any_sync(active, rank);
+  const int leader = __ffs(peers) - 1, lane = threadIdx.x & 31;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(&count[rank], __popc(peers));
+  base = __shfl_sync(peers, base, leader);
+  inCell[a] = base + __popc(peers & ((1u << lane) - 1u));
 }
 
 // three-phase device-wide exclusive scan (counts -> starts), starts[n] = total
@@ -211,25 +219,35 @@ static void device_scan(System& s, const int* in, int* out, int n) {
   CK(cudaGetLastError());
 }
 
-__global__ void k_scatter(const int4* atomK, int N, const int* start, int* cursor, int* orig) {
+__global__ void k_scatter(const int4* atomK, int N, const int* start, const int* inCell, int* orig) {
   int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= N) return;
-  int rank = atomK[a].w;
-  orig[start[rank] + atomicAdd(&cursor[rank], 1)] = a;
+  orig[start[atomK[a].w] + inCell[a]] = a;
 }
 
-// deterministic order inside a cell: ascending atom index
-__global__ void k_sort_cells(const int* start, int nRanks, int* orig) {
+// Order inside a cell: ascending cell-local x coordinate u.x (computed as in
+// k_pack_mixed, so the build's staged positions are sorted along x within
+// every cell and hence along every stencil row), ties by ascending atom index.
+// Deterministic for given coordinates.
+__global__ void k_sort_cells(const int* start, int nRanks, int* orig, const double* __restrict__ R,
+                             const int4* __restrict__ atomK, double scale, float* key) {
   int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= nRanks) return;
   int b = start[r], e = start[r + 1];
+  for (int i = b; i < e; i++) {
+    int a = orig[i];
+    key[i] = (float)(R[3 * a] * scale - (double)atomK[a].x);
+  }
   for (int i = b + 1; i < e; i++) {
     int v = orig[i], j = i - 1;
-    while (j >= b && orig[j] > v) {
+    float kv = key[i];
+    while (j >= b && (key[j] > kv || (key[j] == kv && orig[j] > v))) {
       orig[j + 1] = orig[j];
+      key[j + 1] = key[j];
       j--;
     }
     orig[j + 1] = v;
+    key[j + 1] = kv;
   }
 }
 
@@ -420,10 +438,28 @@ __global__ void __launch_bounds__(BUILD_THREADS) k_build(BuildArgs A) {
     for (int pass = 0; pass <= (layered ? 1 : 0) && !none; pass++) {
       // the 5 cells of a stencil row (dx = -2..2) are consecutive in the halo
       for (int row = 0; row < 25; row++) {
-        const int h0 = (hcx - 2) + HW * ((hcy + row % 5 - 2) + HW * (hcz + row / 5 - 2));
+        const int hy = hcy + row % 5 - 2, hz = hcz + row / 5 - 2;
+        const int h0 = (hcx - 2) + HW * (hy + HW * hz);
+        int q = off[h0];
         const int q1 = off[h0 + 5];
-        for (int q = off[h0]; q < q1; q++) {
+        float xhi = 3.0e38f;
+        if (!MINIMG) {
+          // Atoms of a row are sorted along x.  With rho the distance from atom i
+          // to the row's y-z cross-section, only |x_j - x_i| < sqrt(hi2 - rho^2)
+          // can be inside; a 1e-3 cell margin covers the FP32 rounding of the frame.
+          const float y0 = (float)(hy - g.C), z0 = (float)(hz - g.C);
+          const float dy = fmaxf(fmaxf(y0 - pi.y, pi.y - (y0 + 1.0f)) - 1e-3f, 0.0f);
+          const float dz = fmaxf(fmaxf(z0 - pi.z, pi.z - (z0 + 1.0f)) - 1e-3f, 0.0f);
+          const float rem = A.hi2 - (dy * dy + dz * dz);
+          if (rem <= 0.0f) continue;
+          const float w = sqrtf(rem) + 1e-3f;
+          const float xlo = pi.x - w;
+          xhi = pi.x + w;
+          while (q < q1 && hpos[q].x <= xlo) q++;
+        }
+        for (; q < q1; q++) {
           const float4 pj = hpos[q];
+          if (!MINIMG && pj.x >= xhi) break;
           float ex = pi.x - pj.x, ey = pi.y - pj.y, ez = pi.z - pj.z;
           if (MINIMG) {
             ex -= A.Mf * rintf(ex / A.Mf);
@@ -500,13 +536,10 @@ void device_build_lists(System& s) {
     g.nRanks = g.nTiles * TB * TB * TB;
     g.haloCells = geo.haloCells;
     grow(g.dCount, c.ranks, (size_t)g.nRanks + 1);
-    // dStart / dCursor share the rank capacity
     if (!g.dStart || c.scan < (size_t)g.nRanks + 1) {
       CK(cudaFree(g.dStart));
-      CK(cudaFree(g.dCursor));
       CK(cudaFree(g.dScanTmp));
       CK(cudaMalloc(&g.dStart, sizeof(int) * (g.nRanks + 1)));
-      CK(cudaMalloc(&g.dCursor, sizeof(int) * (g.nRanks + 1)));
       CK(cudaMalloc(&g.dScanTmp, sizeof(int) * ((g.nRanks + SCAN_TILE) / SCAN_TILE + 1)));
       c.scan = (size_t)g.nRanks + 1;
     }
@@ -516,6 +549,8 @@ void device_build_lists(System& s) {
       CK(cudaFree(g.dSelf));
       CK(cudaFree(g.dSlotOf));
       CK(cudaFree(g.dAtomKd));
+      CK(cudaFree(g.dKeyX));
+      CK(cudaMalloc(&g.dKeyX, sizeof(float) * N));
       CK(cudaMalloc(&g.dSlotOf, sizeof(int) * N));
       CK(cudaMalloc(&g.dAtomKd, sizeof(double) * 3 * N));
       CK(cudaMalloc(&g.dOrig, sizeof(int) * N));
@@ -536,13 +571,14 @@ void device_build_lists(System& s) {
     }
     int th = 256, bl = (N + th - 1) / th;
     CK(cudaMemsetAsync(g.dCount, 0, sizeof(int) * (g.nRanks + 1), s.stream));
-    CK(cudaMemsetAsync(g.dCursor, 0, sizeof(int) * (g.nRanks + 1), s.stream));
     s.prof.total += 8;   // assign, 3 scan phases, scatter, sort, fill, tile info
-    k_assign<<<bl, th, 0, s.stream>>>(s.dR, N, 1.0 / L, geo, g.dAtomK, g.dAtomKd, g.dCount);
+    // the slot array holds each atom's place in its cell until k_fill_slots
+    k_assign<<<bl, th, 0, s.stream>>>(s.dR, N, 1.0 / L, geo, g.dAtomK, g.dAtomKd, g.dCount, g.dSlotOf);
     CK(cudaGetLastError());
     device_scan(s, g.dCount, g.dStart, g.nRanks);
-    k_scatter<<<bl, th, 0, s.stream>>>(g.dAtomK, N, g.dStart, g.dCursor, g.dOrig);
-    k_sort_cells<<<(g.nRanks + 255) / 256, 256, 0, s.stream>>>(g.dStart, g.nRanks, g.dOrig);
+    k_scatter<<<bl, th, 0, s.stream>>>(g.dAtomK, N, g.dStart, g.dSlotOf, g.dOrig);
+    k_sort_cells<<<(g.nRanks + 255) / 256, 256, 0, s.stream>>>(g.dStart, g.nRanks, g.dOrig, s.dR, g.dAtomK,
+                                                               (double)M / L, g.dKeyX);
     k_fill_slots<<<bl, th, 0, s.stream>>>(g.dOrig, N, g.dAtomK, s.dType, g.dK, g.dType8, g.dSlotOf);
     int* dMax = g.dTileInfo + 2 * g.nTiles;
     CK(cudaMemsetAsync(dMax, 0, sizeof(int) * 4, s.stream));
@@ -551,17 +587,6 @@ void device_build_lists(System& s) {
     int hmax[2];
     CK(cudaMemcpyAsync(hmax, dMax, sizeof(int) * 2, cudaMemcpyDeviceToHost, s.stream));
     CK(cudaStreamSynchronize(s.stream));
-    {
-      size_t need = (size_t)g.nTiles * g.haloCells;
-      if (g.haloTabCap < need) {
-        CK(cudaFree(g.dHaloTab));
-        CK(cudaMalloc(&g.dHaloTab, sizeof(int2) * need));
-        g.haloTabCap = need;
-      }
-      k_halo_table<<<g.nTiles, 128, 0, s.stream>>>(geo, g.dHaloTab);
-      CK(cudaGetLastError());
-      s.prof.total++;
-    }
     g.tileStride = std::max(32, (hmax[0] + 31) / 32 * 32);
     g.maxHalo = hmax[1];
     size_t smem = build_smem(g, s.ntypes);
@@ -574,6 +599,19 @@ void device_build_lists(System& s) {
     break;
   }
   TileGeom geo = make_geom(g.M, g.TB);
+  if (g.tabM != g.M || g.tabTB != g.TB) {   // the halo table depends on the geometry only
+    size_t need = (size_t)g.nTiles * g.haloCells;
+    if (g.haloTabCap < need) {
+      CK(cudaFree(g.dHaloTab));
+      CK(cudaMalloc(&g.dHaloTab, sizeof(int2) * need));
+      g.haloTabCap = need;
+    }
+    k_halo_table<<<g.nTiles, 128, 0, s.stream>>>(geo, g.dHaloTab);
+    CK(cudaGetLastError());
+    s.prof.total++;
+    g.tabM = g.M;
+    g.tabTB = g.TB;
+  }
   // neighbor capacity: expected full-list count with margin, grown on overflow
   if (g.cap == 0) {
     double rho = N / (L * L * L);

@@ -114,13 +114,14 @@ struct Grid {
   int tileStride = 0;   // max atoms per tile, padded to a multiple of 32
   int maxHalo = 0;      // max halo atoms over tiles
   size_t nbBytes = 0;
-  int *dCount = nullptr, *dStart = nullptr, *dCursor = nullptr, *dScanTmp = nullptr;
+  int *dCount = nullptr, *dStart = nullptr, *dScanTmp = nullptr;
   int* dOrig = nullptr;
   uint16_t* dSelf = nullptr;   // halo index of each slot in its own tile
   int4* dK = nullptr;
   int4* dAtomK = nullptr;
   int* dSlotOf = nullptr;   // atom -> slot of the last build
   double* dAtomKd = nullptr;   // the build-time unwrapped cell of each atom, as doubles
+  float* dKeyX = nullptr;      // sort key of each slot (cell-local x) during a build
   float4* dPos4 = nullptr;
   uint8_t* dType8 = nullptr;
   double* dRs64 = nullptr;
@@ -129,6 +130,7 @@ struct Grid {
   int* dTileInfo = nullptr;   // per tile: atoms, halo atoms
   int2* dHaloTab = nullptr;   // per tile and halo cell: rank, packed halo coordinates
   size_t haloTabCap = 0;
+  int tabM = 0, tabTB = 0;    // geometry the halo table was written for
   GridCaps caps;
 };
 
@@ -256,6 +258,7 @@ void device_pack(System& s);
 void device_pair_forces(System& s, bool compute);
 // P <- CP P + CF F (free atoms); optional 2KE per dimension into hResult[10..12].
 void device_boost(System& s, double CP, double CF, bool kinetic);
+void device_kinetic(System& s, double* twoKE);   // free atoms only (no bodies)
 // R <- CR R + CP P / m (free atoms).
 void device_move(System& s, double CR, double CP);
 // pending boosts + move (CR = 1) + skin displacement + FP32 packing in one pass
