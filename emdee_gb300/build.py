@@ -33,6 +33,7 @@ UNITS = {
     "ewald.cu": ["-fmad=false"],
     "verlet.cu": ["-fmad=false"],
     "replicas.cu": ["-fmad=false"],
+    "bonded.cu": ["-fmad=false"],
     "surrogate.cu": [],
 }
 HEADERS = ["system.hpp", "pairmath.cuh", "tile.cuh", "reduce.cuh", "rigid.cuh", "bodies.cuh", os.path.join("..", "..", "include", "emdee.h")]

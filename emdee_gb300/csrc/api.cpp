@@ -299,12 +299,15 @@ static void compute_forces_impl(tEmDee* md) {
   s.skinReady = s.packReady = false;
   device_pair_forces(s, compute);
   const double* r = s.hResult;   // Epair, Ecoul, Wpair, Wcoul
+  double bonded[5];   // Ebond, Wbond, Eangle, Wangle, Coulomb discounts of bonds and angles
+  device_bonded(s, bonded);
+  const double Ecoul = r[1] + bonded[4];
   double Elong = 0.0, Wlong = 0.0;
   if (s.coul[s.layer - 1].requires_kspace) {   // src/EmDeeCode.f90:1249-1252
     Elong = ewald_compute(s);
-    Wlong = r[1] + Elong - r[3];
+    Wlong = Ecoul + Elong - r[3];
   }
-  md->Virial.Total = r[2] + r[3] + Wlong + 0.0 + 0.0;
+  md->Virial.Total = r[2] + r[3] + Wlong + bonded[1] + bonded[3];
   md->Virial.Body = 0.0;
   if (s.nbodies != 0) {   // src/EmDeeData.f90:926-953
     md->Virial.Body = bodies_virial(s);
@@ -312,10 +315,10 @@ static void compute_forces_impl(tEmDee* md) {
   }
   if (compute) {
     md->Energy.Dispersion = r[0];
-    md->Energy.Coulomb = r[1] + Elong;
-    md->Energy.Bond = 0.0;
-    md->Energy.Angle = 0.0;
-    md->Energy.Potential = r[0] + r[1] + Elong + 0.0 + 0.0;
+    md->Energy.Coulomb = Ecoul + Elong;
+    md->Energy.Bond = bonded[0];
+    md->Energy.Angle = bonded[2];
+    md->Energy.Potential = r[0] + Ecoul + Elong + bonded[0] + bonded[2];
     md->Energy.ShadowPotential = md->Energy.Potential;
   }
   md->Energy.UpToDate = compute;
@@ -562,6 +565,7 @@ void EmDee_destroy(tEmDee* md) {
   cudaFree(s->dExFirst);
   cudaFree(s->dExCount);
   cudaFree(s->dExItem);
+  bonded_free(*s);
   Grid& g = s->grid;
   cudaFree(g.dCount); cudaFree(g.dStart); cudaFree(g.dScanTmp); cudaFree(g.dOrig);
   cudaFree(g.dSelf); cudaFree(g.dK); cudaFree(g.dAtomK); cudaFree(g.dPos4); cudaFree(g.dType8);
@@ -736,23 +740,60 @@ void EmDee_ignore_pair(tEmDee md, int i, int j) {
     for (int k = a; k < s.natoms; k++) s.exFirst[k]++;
     for (int k = a - 1; k < s.natoms; k++) s.exLast[k]++;
   }
-  if (s.initialized) {
-    upload_exclusions(s);
-    s.r0Valid = false;
-  }
+  // the lists change at the next rebuild, as in the reference
+  if (s.initialized) upload_exclusions(s);
 }
 
+// src/EmDeeCode.f90:574-655: the item is stored and its atom pairs excluded
 void EmDee_add_bond(tEmDee md, int i, int j, void* model) {
-  (void)md; (void)i; (void)j; (void)model;
-  fatal("add_bond", "bonded terms are outside the GB300 force path");
+  System& s = *sys_of(md);
+  if (!ranged(i, s.natoms) || !ranged(j, s.natoms)) fatal("add_bond", "atom index out of range");
+  if (!model) fatal("add_bond", "a valid model must be provided");
+  const Model& m = *(const Model*)model;
+  if (m.cls != MC_BOND) fatal("add_bond", "the provided model must be a bond model");
+  BondedTerms::Item b;
+  b.i = i - 1;
+  b.j = j - 1;
+  b.kind = m.kind == MK_BOND_HARMONIC ? 1 : 0;
+  b.kf = m.k;
+  b.x0 = m.x0;
+  s.bondedTerms.bonds.push_back(b);
+  EmDee_ignore_pair(md, i, j);
 }
+
 void EmDee_add_angle(tEmDee md, int i, int j, int k, void* model) {
-  (void)md; (void)i; (void)j; (void)k; (void)model;
-  fatal("add_angle", "bonded terms are outside the GB300 force path");
+  System& s = *sys_of(md);
+  if (!ranged(i, s.natoms) || !ranged(j, s.natoms) || !ranged(k, s.natoms))
+    fatal("add_angle", "atom index out of range");
+  if (!model) fatal("add_angle", "a valid model must be provided");
+  const Model& m = *(const Model*)model;
+  if (m.cls != MC_ANGLE) fatal("add_angle", "the provided model must be an angle model");
+  BondedTerms::Item a;
+  a.i = i - 1;
+  a.j = j - 1;
+  a.k = k - 1;
+  a.kind = m.kind == MK_ANGLE_HARMONIC ? 1 : 0;
+  a.kf = m.k;
+  a.x0 = m.x0;
+  s.bondedTerms.angles.push_back(a);
+  EmDee_ignore_pair(md, i, j);
+  EmDee_ignore_pair(md, i, k);
+  EmDee_ignore_pair(md, j, k);
 }
+
 void EmDee_add_dihedral(tEmDee md, int i, int j, int k, int l, void* model) {
-  (void)md; (void)i; (void)j; (void)k; (void)l; (void)model;
-  fatal("add_dihedral", "bonded terms are outside the GB300 force path");
+  System& s = *sys_of(md);
+  if (!ranged(i, s.natoms) || !ranged(j, s.natoms) || !ranged(k, s.natoms) || !ranged(l, s.natoms))
+    fatal("add_dihedral", "atom index out of range");
+  if (!model) fatal("add_dihedral", "a valid model must be provided");
+  if (((const Model*)model)->cls != MC_DIHEDRAL) fatal("add_dihedral", "the provided model must be a dihedral model");
+  s.bondedTerms.ndihedrals++;
+  EmDee_ignore_pair(md, i, j);
+  EmDee_ignore_pair(md, i, k);
+  EmDee_ignore_pair(md, i, l);
+  EmDee_ignore_pair(md, j, k);
+  EmDee_ignore_pair(md, j, l);
+  EmDee_ignore_pair(md, k, l);
 }
 
 // src/EmDeeCode.f90:805-925

@@ -77,6 +77,7 @@ __global__ void __launch_bounds__(PAIR_THREADS) k_pair_mixed(PairArgsF A) {
 
   NBParams<float> m0 = A.table[0].model;
   if (VAR == 0) m0.modifier = MOD;
+  const float sigc = m0.sigsq * A.invw2, eps48 = 2.0f * m0.eps24;
   NBParams<float> coul;
   if (VAR == 1) coul = *A.coul;
   const int tb = A.start[t * cells], te = A.start[(t + 1) * cells];
@@ -116,8 +117,10 @@ __global__ void __launch_bounds__(PAIR_THREADS) k_pair_mixed(PairArgsF A) {
           const float invR2c = Ops<float>::rcp(r2);
           const float invR2 = invR2c * A.invw2;
           const float invR = needR ? sqrtf(invR2) : 1.f;
-          const float sr2 = m0.sigsq * invR2, sr6 = sr2 * sr2 * sr2, sr12 = sr6 * sr6;
-          float E = m0.eps4 * (sr12 - sr6), W = m0.eps24 * (sr12 + sr12 - sr6);
+          // sr2 = sigma^2 / r^2 with r in cell units; E = 4 eps sr6 (sr6 - 1),
+          // W = 24 eps sr6 (2 sr6 - 1)
+          const float sr2 = sigc * invR2c, sr6 = sr2 * sr2 * sr2;
+          float E = sr6 * fmaf(m0.eps4, sr6, -m0.eps4), W = sr6 * fmaf(eps48, sr6, -m0.eps24);
           if (MOD != NONE) modifier_compute(m0, E, W, invR, invR2);
           W = in ? W : 0.f;
           if (COUNT) within += in ? 1.f : 0.f;

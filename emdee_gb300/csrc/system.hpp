@@ -105,6 +105,22 @@ struct VerletScratch {
   size_t s0Cap = 0, r0Cap = 0, q0Cap = 0, partBCap = 0, partFCap = 0;
 };
 
+// Bonds and angles (src/structs.f90, src/EmDeeData.f90:443-550): host lists in the
+// order they were added (0-based atoms) and their device tables.
+struct BondedTerms {
+  struct Item {
+    int i = 0, j = 0, k = -1, kind = 0;   // kind: 0 none, 1 harmonic
+    double kf = 0, x0 = 0;                // force constant, equilibrium length or angle
+  };
+  std::vector<Item> bonds, angles;
+  int ndihedrals = 0;   // stored for their exclusions only
+  int uploaded = 0;     // items on the device
+  int4* dItem = nullptr;
+  double2* dParam = nullptr;
+  double *dQQ = nullptr, *dVec = nullptr, *dPartials = nullptr;
+  int *dFirst = nullptr, *dEntry = nullptr;
+};
+
 struct Grid {
   int M = 0;            // cells per dimension (src/neighbor_lists.f90:185-186)
   int TB = 0;           // tile edge in cells
@@ -187,6 +203,7 @@ struct System {
   bool kspace_active = false;
   Ewald ewald;
   VerletScratch verlet;
+  BondedTerms bondedTerms;
   std::vector<char> multilayer, overridable, interact, pairs_exist, useInRc, bonded, forcesUpToDate;
   std::vector<tEnergy> layerEnergy;
   std::vector<tVirial> layerVirial;
@@ -259,6 +276,10 @@ void device_pair_forces(System& s, bool compute);
 // P <- CP P + CF F (free atoms); optional 2KE per dimension into hResult[10..12].
 void device_boost(System& s, double CP, double CF, bool kinetic);
 void device_kinetic(System& s, double* twoKE);   // free atoms only (no bodies)
+// bonds and angles of the current layer: adds their forces to F and returns
+// Ebond, Wbond, Eangle, Wangle and the Coulomb discount energy; false if none ran
+bool device_bonded(System& s, double out[5]);
+void bonded_free(System& s);
 // R <- CR R + CP P / m (free atoms).
 void device_move(System& s, double CR, double CP);
 // pending boosts + move (CR = 1) + skin displacement + FP32 packing in one pass

@@ -739,6 +739,11 @@ typedef struct {
 
 #include "ewald_oracle.h"
 
+typedef struct {   /* tStruct (src/structs.f90): atoms (1-based) and a copy of the model */
+  int i, j, k, l;
+  omodel model;
+} ostruct;
+
 typedef struct {
   int natoms, mcells, ncells, maxcells, maxatoms, ntypes, nbodies, nfree, nthreads, threadAtoms;
   int threadFreeAtoms, nlayers, layer;
@@ -770,6 +775,9 @@ typedef struct {
   int ownsR;
   obody* body;
   int threadBodies;
+  /* bonded structures (src/structs.f90): bonds, angles, dihedrals in insertion order */
+  ostruct *bonds, *angles;
+  int nbonds, capbonds, nangles, capangles, ndihedrals;
 } odata;
 
 #define PAIR(me, i, j, l) ((me)->pair[((size_t)(l) * (me)->ntypes + (j)) * (me)->ntypes + (i)])
@@ -1175,17 +1183,57 @@ void EmDee_ignore_pair(tEmDee md, int i, int j) {
   }
 }
 
+/* src/structs.f90:40-60 (structList_add) */
+static void struct_add(ostruct** list, int* n, int* cap, int i, int j, int k, int l, const omodel* model) {
+  if (*n == *cap) {
+    *cap += EXTRA;
+    *list = (ostruct*)realloc(*list, sizeof(ostruct) * (size_t)(*cap));
+  }
+  ostruct* it = &(*list)[(*n)++];
+  it->i = i;
+  it->j = j;
+  it->k = k;
+  it->l = l;
+  it->model = *model;
+}
+
+/* src/EmDeeCode.f90:574-596 */
 void EmDee_add_bond(tEmDee md, int i, int j, void* model) {
-  (void)md; (void)i; (void)j; (void)model;
-  error("add_bond", "bonded terms are outside the accelerated path");
+  odata* me = get(md);
+  if (!ranged(i, me->natoms) || !ranged(j, me->natoms)) error("add_bond", "atom index out of range");
+  if (!model) error("add_bond", "a valid model must be provided");
+  if (((omodel*)model)->cls != MC_BOND) error("add_bond", "the provided model must be a bond model");
+  struct_add(&me->bonds, &me->nbonds, &me->capbonds, i, j, 0, 0, (omodel*)model);
+  EmDee_ignore_pair(md, i, j);
 }
+
+/* src/EmDeeCode.f90:600-624 */
 void EmDee_add_angle(tEmDee md, int i, int j, int k, void* model) {
-  (void)md; (void)i; (void)j; (void)k; (void)model;
-  error("add_angle", "bonded terms are outside the accelerated path");
+  odata* me = get(md);
+  if (!ranged(i, me->natoms) || !ranged(j, me->natoms) || !ranged(k, me->natoms))
+    error("add_angle", "atom index out of range");
+  if (!model) error("add_angle", "a valid model must be provided");
+  if (((omodel*)model)->cls != MC_ANGLE) error("add_angle", "the provided model must be an angle model");
+  struct_add(&me->angles, &me->nangles, &me->capangles, i, j, k, 0, (omodel*)model);
+  EmDee_ignore_pair(md, i, j);
+  EmDee_ignore_pair(md, i, k);
+  EmDee_ignore_pair(md, j, k);
 }
+
+/* src/EmDeeCode.f90:628-655; the reference never evaluates dihedrals */
 void EmDee_add_dihedral(tEmDee md, int i, int j, int k, int l, void* model) {
-  (void)md; (void)i; (void)j; (void)k; (void)l; (void)model;
-  error("add_dihedral", "bonded terms are outside the accelerated path");
+  odata* me = get(md);
+  if (!ranged(i, me->natoms) || !ranged(j, me->natoms) || !ranged(k, me->natoms) || !ranged(l, me->natoms))
+    error("add_dihedral", "atom index out of range");
+  if (!model) error("add_dihedral", "a valid model must be provided");
+  if (((omodel*)model)->cls != MC_DIHEDRAL) error("add_dihedral", "the provided model must be a dihedral model");
+  me->ndihedrals++;
+  EmDee_ignore_pair(md, i, j);
+  EmDee_ignore_pair(md, i, k);
+  EmDee_ignore_pair(md, i, l);
+  EmDee_ignore_pair(md, j, k);
+  EmDee_ignore_pair(md, j, l);
+  EmDee_ignore_pair(md, k, l);
 }
 
 /* src/EmDeeData.f90:193-223 */
@@ -1503,6 +1551,103 @@ static void compute_pairs(odata* me, int thread, int compute, const double* Rs, 
   for (size_t q = 0; q < (size_t)3 * me->natoms; q++) F[q] = L * F[q];
 }
 
+/* compute_bonds (src/EmDeeData.f90:443-487) with bond_harmonic (src/bond_harmonic.f90:64-75) */
+static void compute_bonds(odata* me, int thread, const double* R, double* F, double* Potential, double* Virial,
+                          double* Ecoul) {
+  int layer = me->layer, bonded = me->bonded[layer - 1], kspace = me->coul[layer - 1].requires_kspace;
+  if (!(me->nbonds > 0 && (bonded || kspace))) return;
+  int per = (me->nbonds + me->nthreads - 1) / me->nthreads;
+  double L = *me->Lbox, invL2 = 1.0 / (L * L);
+  int last = thread * per < me->nbonds ? thread * per : me->nbonds;
+  for (int m = (thread - 1) * per + 1; m <= last; m++) {
+    const ostruct* b = &me->bonds[m - 1];
+    double Rij[3];
+    for (int d = 0; d < 3; d++) Rij[d] = pbc(R[3 * (b->i - 1) + d] - R[3 * (b->j - 1) + d]);
+    double invR2 = invL2 / (Rij[0] * Rij[0] + Rij[1] * Rij[1] + Rij[2] * Rij[2]);
+    double E = 0.0, W = 0.0;
+    if (bonded) {
+      if (b->model.kind == MK_BOND_HARMONIC) {
+        double r = 1.0 / sqrt(invR2), delta = r - b->model.x0;
+        E = (0.5 * b->model.k) * (delta * delta);
+        W = (-b->model.k) * delta * r;
+      }
+      *Potential += E;
+      *Virial += W;
+    } else {
+      W = 0.0;
+    }
+    if (kspace) {
+      int itype = me->atomType[b->i - 1], jtype = me->atomType[b->j - 1];
+      double QiQj = PAIR(me, itype - 1, jtype - 1, layer - 1).kCoul * me->charge[b->i - 1] * me->charge[b->j - 1];
+      double EL, WL;
+      ewald_discount(&me->ewald, &EL, &WL, 1.0 / invR2, QiQj);
+      *Ecoul += EL;
+      W = W + WL;
+    }
+    for (int d = 0; d < 3; d++) {
+      double Fij = W * invR2 * L * Rij[d];
+      F[3 * (b->i - 1) + d] += Fij;
+      F[3 * (b->j - 1) + d] -= Fij;
+    }
+  }
+}
+
+/* compute_angles (src/EmDeeData.f90:491-550) with angle_harmonic (src/angle_harmonic.f90:64-73) */
+static void compute_angles(odata* me, int thread, const double* R, double* F, double* Potential, double* Virial,
+                           double* Ecoul) {
+  int layer = me->layer, bonded = me->bonded[layer - 1], kspace = me->coul[layer - 1].requires_kspace;
+  if (!(me->nangles > 0 && (bonded || kspace))) return;
+  int per = (me->nangles + me->nthreads - 1) / me->nthreads;
+  double L = *me->Lbox;
+  int last = thread * per < me->nangles ? thread * per : me->nangles;
+  for (int m = (thread - 1) * per + 1; m <= last; m++) {
+    const ostruct* g = &me->angles[m - 1];
+    int i = g->i, j = g->j, k = g->k;
+    double a[3], b[3];
+    for (int d = 0; d < 3; d++) {
+      a[d] = L * pbc(R[3 * (i - 1) + d] - R[3 * (j - 1) + d]);
+      b[d] = L * pbc(R[3 * (k - 1) + d] - R[3 * (j - 1) + d]);
+    }
+    if (bonded) {
+      double aa = a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
+      double bb = b[0] * b[0] + b[1] * b[1] + b[2] * b[2];
+      double ab = a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+      double theta = acos(ab / sqrt(aa * bb)), Ea = 0.0, Fa = 0.0;
+      if (g->model.kind == MK_ANGLE_HARMONIC) {
+        double delta = theta - g->model.x0;
+        Ea = (0.5 * g->model.k) * (delta * delta);
+        Fa = (-g->model.k) * delta;
+      }
+      double factor = Fa / sqrt(aa * bb - ab * ab), Fi[3], Fk[3], v = 0.0;
+      for (int d = 0; d < 3; d++) {
+        Fi[d] = ((ab / aa) * a[d] - b[d]) * factor;
+        Fk[d] = ((ab / bb) * b[d] - a[d]) * factor;
+      }
+      for (int d = 0; d < 3; d++) {
+        F[3 * (i - 1) + d] += Fi[d];
+        F[3 * (k - 1) + d] += Fk[d];
+        F[3 * (j - 1) + d] -= Fi[d] + Fk[d];
+        v += Fi[d] * a[d] + Fk[d] * b[d];
+      }
+      *Potential += Ea;
+      *Virial += v;
+    }
+    if (kspace) {
+      double Rik[3] = {a[0] - b[0], a[1] - b[1], a[2] - b[2]};
+      double RikSq = Rik[0] * Rik[0] + Rik[1] * Rik[1] + Rik[2] * Rik[2], EL, WL;
+      int itype = me->atomType[i - 1], ktype = me->atomType[k - 1];
+      double QiQk = PAIR(me, itype - 1, ktype - 1, layer - 1).kCoul * me->charge[i - 1] * me->charge[k - 1];
+      ewald_discount(&me->ewald, &EL, &WL, RikSq, QiQk);
+      *Ecoul += EL;
+      for (int d = 0; d < 3; d++) {
+        double Fik = WL * Rik[d] / RikSq;
+        F[3 * (i - 1) + d] += Fik;
+        F[3 * (k - 1) + d] -= Fik;
+      }
+    }
+  }
+}
+
 /* ======================================================================== */
 /* EmDee_compute_forces (src/EmDeeCode.f90:1215-1277)                         */
 /* ======================================================================== */
@@ -1513,7 +1658,7 @@ void EmDee_compute_forces(tEmDee* md) {
   double L = *me->Lbox, E[5] = {0, 0, 0, 0, 0}, W[5] = {0, 0, 0, 0, 0};
   double* Rs = (double*)xmalloc(sizeof(double) * 3 * N);
   double* Fs = (double*)xmalloc(sizeof(double) * 3 * N * nt);
-  double* Et = (double*)xcalloc((size_t)nt * 4, sizeof(double));
+  double* Et = (double*)xcalloc((size_t)nt * 8, sizeof(double));
   int compute = md->Options.Compute;
   for (size_t q = 0; q < (size_t)3 * N; q++) Rs[q] = me->R[q] / L;
   handle_neighbor_lists(me, &md->Builds, &md->Time.Neighbor, Rs);
@@ -1521,14 +1666,21 @@ void EmDee_compute_forces(tEmDee* md) {
 #pragma omp parallel num_threads(nt)
   {
     int thread = omp_get_thread_num() + 1;
-    double* ev = &Et[4 * (thread - 1)];
-    compute_pairs(me, thread, compute, Rs, &Fs[(size_t)3 * N * (thread - 1)], &ev[0], &ev[1], &ev[2], &ev[3]);
+    double* ev = &Et[8 * (thread - 1)];
+    double* Ft = &Fs[(size_t)3 * N * (thread - 1)];
+    compute_pairs(me, thread, compute, Rs, Ft, &ev[0], &ev[1], &ev[2], &ev[3]);
+    compute_bonds(me, thread, Rs, Ft, &ev[4], &ev[5], &ev[1]);
+    compute_angles(me, thread, Rs, Ft, &ev[6], &ev[7], &ev[1]);
   }
   for (int t = 0; t < nt; t++) {   /* OpenMP reduction(+:E,W), taken in thread order */
-    E[0] += Et[4 * t];
-    E[1] += Et[4 * t + 1];
-    W[0] += Et[4 * t + 2];
-    W[1] += Et[4 * t + 3];
+    E[0] += Et[8 * t];
+    E[1] += Et[8 * t + 1];
+    W[0] += Et[8 * t + 2];
+    W[1] += Et[8 * t + 3];
+    E[3] += Et[8 * t + 4];
+    W[3] += Et[8 * t + 5];
+    E[4] += Et[8 * t + 6];
+    W[4] += Et[8 * t + 7];
   }
   for (size_t q = 0; q < (size_t)3 * N; q++) {   /* me%F = sum(Fs,3) */
     double s = Fs[q];

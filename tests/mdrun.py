@@ -83,14 +83,35 @@ COUL_MODELS = {
     "coul_shifted_square_smoothed": lambda lib: lib.EmDee_coul_shifted_square_smoothed(1.0),
     "shifted_force(coul_damped)": lambda lib: lib.EmDee_shifted_force(lib.EmDee_coul_damped(0.2)),
     "square_smoothed(coul_cut)": lambda lib: lib.EmDee_square_smoothed(lib.EmDee_coul_cut(), 1.0),
+    "none": lambda lib: lib.EmDee_coul_none(),
 }
 
 
+# SPC/Fw flexible water (Wu, Tepper and Voth, J. Chem. Phys. 124, 024503 (2006)):
+# O-H bonds and the H-O-H angle, force constants in kcal/mol per A^2 and per rad^2
+SPCFW = dict(kb=1059.162, r0=1.012, ka=75.90, theta0=np.radians(113.24))
+
+
+def add_flexible_water(lib, md, natoms, mvv2e, kb=None, ka=None):
+    """Harmonic O-H bonds and H-O-H angles for molecules laid out as O, H, H
+    (EmDee_add_bond / EmDee_add_angle, src/EmDeeCode.f90:574-624); these also
+    exclude the intramolecular pairs from the neighbor lists."""
+    bond = lib.EmDee_bond_harmonic((kb or SPCFW["kb"]) / mvv2e, SPCFW["r0"])
+    angle = lib.EmDee_angle_harmonic((ka or SPCFW["ka"]) / mvv2e, SPCFW["theta0"])
+    for m in range(natoms // 3):
+        o, h1, h2 = 3 * m + 1, 3 * m + 2, 3 * m + 3
+        lib.EmDee_add_bond(md, o, h1, bond)
+        lib.EmDee_add_bond(md, o, h2, bond)
+        lib.EmDee_add_angle(md, h1, o, h2, angle)
+
+
 def setup_water(lib, cfg, coul, pair="shifted_force", precision=None, natoms=None, exclusions=True,
-                rigid=False, coords_first=False):
+                rigid=False, coords_first=False, flexible=False, hook=None):
     """SPC/E sample (test/test_coul_*.f90:33-48): O-O Lennard-Jones (H:
     pair_none) and the Coulomb model `coul`.  With rigid=False the molecules are
-    free atoms whose intramolecular pairs are excluded with EmDee_ignore_pair;
+    free atoms whose intramolecular pairs are excluded with EmDee_ignore_pair
+    (flexible=True: with SPC/Fw bonds and angles, which exclude them instead;
+    hook(lib, md), if given, runs after the models are set, before initialization);
     with rigid=True each molecule is a rigid body (EmDee_system's `bodies`
     argument, test/test_rigid_body_exact.f90:35), which drops its internal pairs
     from the neighbor lists.  coords_first uploads the coordinates before the box
@@ -103,7 +124,7 @@ def setup_water(lib, cfg, coul, pair="shifted_force", precision=None, natoms=Non
     if precision is not None:
         lib.EmDee_set_precision(md, precision)
     for i, (eps, sig) in enumerate(zip(cfg["epsilon"], cfg["sigma"])):
-        if eps == 0.0:
+        if eps == 0.0 or pair == "none":
             p = lib.EmDee_pair_none()
         elif pair == "softcore":
             p = lib.EmDee_pair_softcore_cut(eps / run["mvv2e"], sig, 0.7)
@@ -111,7 +132,9 @@ def setup_water(lib, cfg, coul, pair="shifted_force", precision=None, natoms=Non
             p = lib.EmDee_shifted_force(lib.EmDee_pair_lj_cut(eps / run["mvv2e"], sig))
         lib.EmDee_set_pair_model(md, i + 1, i + 1, p, run["kCoul"])
     lib.EmDee_set_coul_model(md, COUL_MODELS[coul](lib))
-    if exclusions and not rigid:
+    if flexible:
+        add_flexible_water(lib, md, N, run["mvv2e"])
+    elif exclusions and not rigid:
         mol = cfg["molecule"][:N]
         first = {}
         for a, m in enumerate(mol):
@@ -120,6 +143,8 @@ def setup_water(lib, cfg, coul, pair="shifted_force", precision=None, natoms=Non
             for x in range(len(atoms)):
                 for y in range(x + 1, len(atoms)):
                     lib.EmDee_ignore_pair(md, atoms[x], atoms[y])
+    if hook is not None:
+        hook(lib, md)
     lib.upload(md, "charges", cfg["charge"][:N])
     if coords_first:
         lib.upload(md, "coordinates", np.array(cfg["coordinates"][:N]))

@@ -16,7 +16,7 @@ import numpy as np
 import pytest
 
 from emdee_gb300.emdee import EmDee
-from mdrun import load_golden
+from mdrun import add_flexible_water, load_golden
 
 MADELUNG_NACL = 1.747564594633182   # nearest-neighbour convention
 
@@ -47,7 +47,7 @@ def rock_salt(lib, n, acc, precision=None):
     return md, len(g)
 
 
-def ewald_water(lib, w, acc, natoms=None, rigid=False, precision=None, rc=10.0):
+def ewald_water(lib, w, acc, natoms=None, rigid=False, precision=None, rc=10.0, flexible=False):
     run = w["run"]
     N = natoms or len(w["coordinates"])
     md = lib.system(1, 1, rc, 2.0, N, w["type"][:N], w["mass"], w["molecule"][:N] if rigid else None)
@@ -59,7 +59,9 @@ def ewald_water(lib, w, acc, natoms=None, rigid=False, precision=None, rc=10.0):
         lib.EmDee_set_pair_model(md, i + 1, i + 1, p, run["kCoul"])
     lib.EmDee_set_coul_model(md, lib.EmDee_coul_long())
     lib.EmDee_set_kspace_model(md, lib.EmDee_kspace_ewald(acc))
-    if not rigid:
+    if flexible:
+        add_flexible_water(lib, md, N, run["mvv2e"])
+    elif not rigid:
         first = {}
         for a, m in enumerate(w["molecule"][:N]):
             first.setdefault(m, []).append(a + 1)
