@@ -51,7 +51,8 @@ def _compile(src, flags, force):
     deps = [os.path.join(CSRC, src)] + [os.path.join(CSRC, h) for h in HEADERS]
     if not force and not _stale(obj, deps):
         return obj, None
-    cmd = [NVCC] + ARCH + COMMON + flags + ["-c", os.path.join(CSRC, src), "-o", obj]
+    extra = os.environ.get("EMDEE_NVCC_FLAGS", "").split()   # tuning defines, e.g. -DPAIR_MIN_BLOCKS=6
+    cmd = [NVCC] + ARCH + COMMON + flags + extra + ["-c", os.path.join(CSRC, src), "-o", obj]
     if src.endswith(".cpp"):
         cmd = [NVCC] + COMMON + ["-x", "c++", "-c", os.path.join(CSRC, src), "-o", obj]
         cmd = [c for c in cmd if c not in ("-lineinfo", "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills")]

@@ -400,8 +400,14 @@ __device__ __forceinline__ size_t nb_index(int t, int capC, int tileStride, int 
 }
 
 // GENERAL: several atom types, bodies, exclusions or layered lists; MINIMG: M = 5.
+// BUILD_MIN_BLOCKS (compile-time): resident blocks per SM the register budget must allow
+#ifdef BUILD_MIN_BLOCKS
+#define BUILD_BOUNDS __launch_bounds__(BUILD_THREADS, BUILD_MIN_BLOCKS)
+#else
+#define BUILD_BOUNDS __launch_bounds__(BUILD_THREADS)
+#endif
 template <bool GENERAL, bool MINIMG>
-__global__ void __launch_bounds__(BUILD_THREADS) k_build(BuildArgs A) {
+__global__ void BUILD_BOUNDS k_build(BuildArgs A) {
   extern __shared__ __align__(16) unsigned char sraw[];
   __shared__ int ws[33];
   const TileGeom g = A.g;
@@ -666,6 +672,9 @@ void device_build_lists(System& s) {
   auto kb = general ? (A.minimg ? k_build<true, true> : k_build<true, false>)
                     : (A.minimg ? k_build<false, true> : k_build<false, false>);
   CK(cudaFuncSetAttribute(kb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+#ifdef EMDEE_MAX_CARVEOUT
+  CK(cudaFuncSetAttribute(kb, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared));
+#endif
   for (int attempt = 0; attempt < 3; attempt++) {
     size_t need = (size_t)g.nTiles * g.cap * g.tileStride;
     grow(g.dNb, c.nb, need);

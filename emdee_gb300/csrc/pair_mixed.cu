@@ -21,6 +21,12 @@
 namespace emdee {
 
 static const int PAIR_THREADS = 256;   // upper bound; launches use one thread per tile atom
+// PAIR_MIN_BLOCKS (compile-time): resident blocks per SM the register budget must allow
+#ifdef PAIR_MIN_BLOCKS
+#define PAIR_BOUNDS __launch_bounds__(PAIR_THREADS, PAIR_MIN_BLOCKS)
+#else
+#define PAIR_BOUNDS __launch_bounds__(PAIR_THREADS)
+#endif
 
 struct PairArgsF {
   TileGeom g;
@@ -54,7 +60,7 @@ struct PairArgsF {
 // the inner loop needs no bounds test (except when M = 5, where the periodic
 // wrap would bring the sentinel back).
 template <bool COMPUTE, int VAR, int MOD, bool MINIMG, bool COUNT>
-__global__ void __launch_bounds__(PAIR_THREADS) k_pair_mixed(PairArgsF A) {
+__global__ void PAIR_BOUNDS k_pair_mixed(PairArgsF A) {
   extern __shared__ __align__(16) unsigned char sraw[];
   __shared__ int ws[33];
   const TileGeom g = A.g;
@@ -154,9 +160,12 @@ __global__ void __launch_bounds__(PAIR_THREADS) k_pair_mixed(PairArgsF A) {
       Fa[2] = f2d_exact(fz * A.invw);
     }
   }
-  // each pair is visited from both atoms: halve the sums
+  // each pair is visited from both atoms: halve the sums.  Sums that are zero by
+  // construction (energies without COMPUTE, Coulomb terms of VAR 0, the count
+  // without COUNT) skip the reduction.
   const float v[5] = {0.5f * Ep, 0.5f * Ec, 0.5f * Wp, 0.5f * Wc, 0.5f * within};
-  grid_reduce_ff<5, PAIR_THREADS>(v, reinterpret_cast<float2*>(A.partials), A.ticket, A.result);
+  constexpr unsigned MASK = (COMPUTE ? (VAR == 1 ? 3u : 1u) : 0u) | (VAR == 1 ? 12u : 4u) | (COUNT ? 16u : 0u);
+  grid_reduce_ff<5, PAIR_THREADS, MASK>(v, reinterpret_cast<float2*>(A.partials), A.ticket, A.result);
 }
 
 template <bool COMPUTE, int VAR, int MOD, bool MINIMG, bool COUNT>
@@ -165,6 +174,9 @@ static void launch(System& s, PairArgsF& A, size_t smem, int nTiles, int threads
   static size_t configured = 0;
   if (smem > configured) {
     CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+#ifdef EMDEE_MAX_CARVEOUT
+    CK(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared));
+#endif
     configured = smem;
   }
   kern<<<nTiles, threads, smem, s.stream>>>(A);

@@ -118,12 +118,15 @@ __device__ __forceinline__ void ff_add(float& hi, float& lo, float bh, float bl)
   lo = lo + bl + err;
 }
 
-template <int NQ>
+// Quantities whose bit is clear in MASK are known to be zero: they skip every
+// level and their result is written as 0.
+template <int NQ, unsigned MASK = ~0u>
 __device__ __forceinline__ void warp_sum_ff(float (&hi)[NQ], float (&lo)[NQ]) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1)
 #pragma unroll
     for (int q = 0; q < NQ; q++) {
+      if (!((MASK >> q) & 1u)) continue;
       const float h2 = __shfl_down_sync(0xffffffffu, hi[q], o), l2 = __shfl_down_sync(0xffffffffu, lo[q], o);
       ff_add(hi[q], lo[q], h2, l2);
     }
@@ -132,7 +135,7 @@ __device__ __forceinline__ void warp_sum_ff(float (&hi)[NQ], float (&lo)[NQ]) {
 // Per-thread FP32 values -> result[q] (FP64).  partials holds NQ float2 per block.
 // The last block (ticket) sums the partials in block order; the result does not
 // depend on block scheduling.
-template <int NQ, int THREADS>
+template <int NQ, int THREADS, unsigned MASK = ~0u>
 __device__ __forceinline__ void grid_reduce_ff(const float (&v)[NQ], float2* partials, unsigned int* ticket,
                                                double* result) {
   __shared__ float2 red[NQ][THREADS / 32];
@@ -144,12 +147,13 @@ __device__ __forceinline__ void grid_reduce_ff(const float (&v)[NQ], float2* par
     hi[q] = v[q];
     lo[q] = 0.f;
   }
-  warp_sum_ff<NQ>(hi, lo);
+  warp_sum_ff<NQ, MASK>(hi, lo);
   if (lane == 0)
 #pragma unroll
-    for (int q = 0; q < NQ; q++) red[q][warp] = make_float2(hi[q], lo[q]);
+    for (int q = 0; q < NQ; q++)
+      if ((MASK >> q) & 1u) red[q][warp] = make_float2(hi[q], lo[q]);
   __syncthreads();
-  if (threadIdx.x < NQ) {
+  if (threadIdx.x < NQ && ((MASK >> threadIdx.x) & 1u)) {
     const int q = threadIdx.x;
     float h = 0.f, l = 0.f;
     for (int w = 0; w < nw; w++) ff_add(h, l, red[q][w].x, red[q][w].y);
@@ -169,18 +173,21 @@ __device__ __forceinline__ void grid_reduce_ff(const float (&v)[NQ], float2* par
   for (unsigned int b = threadIdx.x; b < gridDim.x; b += blockDim.x)
 #pragma unroll
     for (int q = 0; q < NQ; q++) {
+      if (!((MASK >> q) & 1u)) continue;
       const float2 x = __ldcg(&partials[(size_t)b * NQ + q]);
       ff_add(hi[q], lo[q], x.x, x.y);
     }
-  warp_sum_ff<NQ>(hi, lo);
+  warp_sum_ff<NQ, MASK>(hi, lo);
   if (lane == 0)
 #pragma unroll
-    for (int q = 0; q < NQ; q++) red[q][warp] = make_float2(hi[q], lo[q]);
+    for (int q = 0; q < NQ; q++)
+      if ((MASK >> q) & 1u) red[q][warp] = make_float2(hi[q], lo[q]);
   __syncthreads();
   if (threadIdx.x < NQ) {
     const int q = threadIdx.x;
     float h = 0.f, l = 0.f;
-    for (int w = 0; w < nw; w++) ff_add(h, l, red[q][w].x, red[q][w].y);
+    if ((MASK >> q) & 1u)
+      for (int w = 0; w < nw; w++) ff_add(h, l, red[q][w].x, red[q][w].y);
     result[q] = (double)h + (double)l;
   }
   if (threadIdx.x == 0) *ticket = 0;
