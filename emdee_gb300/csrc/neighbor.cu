@@ -143,8 +143,8 @@ bool device_skin_check(System& s) {
 // binning (src/neighbor_lists.f90:122-128) and tile sort
 // ---------------------------------------------------------------------------------
 
-__global__ void k_assign(const double* __restrict__ R, int N, double invL, TileGeom g, int4* atomK, double* atomKd,
-                         int* count, int* inCell) {
+__global__ void k_assign(const double* __restrict__ R, int N, double invL, TileGeom g, int4* atomK, int* count,
+                         int* inCell) {
   int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= N) return;
   int c[3], K[3];
@@ -159,7 +159,6 @@ __global__ void k_assign(const double* __restrict__ R, int N, double invL, TileG
   }
   int rank = cell_rank(g, c[0], c[1], c[2]);
   atomK[a] = make_int4(K[0], K[1], K[2], rank);
-  for (int d = 0; d < 3; d++) atomKd[3 * a + d] = (double)K[d];
   // one atomic per distinct cell of the warp (neighbouring atoms often share a
   // cell); each atom keeps its place among the cell's atoms for the scatter
   const unsigned active = __activemask();
@@ -293,9 +292,11 @@ __global__ void k_tile_info(const int* start, TileGeom g, int* info, int* maxOut
 // per-step packing
 // ---------------------------------------------------------------------------------
 
-// cell-local position of each slot in units of the cell edge: u = M R/L - K
+// cell-local position of each slot in units of the cell edge: u = M R/L - K,
+// and the charge.  At a list build (pos0 != NULL) the same values are also kept
+// per atom as the reference for k_pack_delta and the fused step.
 __global__ void k_pack_mixed(const double* __restrict__ R, const double* __restrict__ charge, const int* orig,
-                             const int4* K, int N, double scale, float4* pos4) {
+                             const int4* K, int N, double scale, float4* pos4, float4* pos0) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= N) return;
   int a = orig[s];
@@ -304,7 +305,26 @@ __global__ void k_pack_mixed(const double* __restrict__ R, const double* __restr
   float uy = (float)(R[3 * a + 1] * scale - (double)k.y);
   float uz = (float)(R[3 * a + 2] * scale - (double)k.z);
   double q = charge[a];
-  pos4[s] = make_float4(ux, uy, uz, fabs(q) > 2.220446049250313e-16 ? (float)q : 0.0f);
+  const float4 v = make_float4(ux, uy, uz, fabs(q) > 2.220446049250313e-16 ? (float)q : 0.0f);
+  pos4[s] = v;
+  if (pos0) pos0[a] = v;
+}
+
+// Between builds, with the box of the last build: u = u0 + (R - R0) M/L, the
+// displacement since the build rounded to FP32 and scaled in FP32 (one FP64
+// subtraction and conversion per coordinate instead of the FP64 M R/L - K).
+// The fused step kernel packs with the same arithmetic.
+__device__ __forceinline__ float4 pack_delta(float4 p0, double dx, double dy, double dz, float scale) {
+  return make_float4(fmaf((float)dx, scale, p0.x), fmaf((float)dy, scale, p0.y), fmaf((float)dz, scale, p0.z), p0.w);
+}
+
+__global__ void k_pack_delta(const double* __restrict__ R, const double* __restrict__ R0, const int* orig,
+                             const float4* __restrict__ pos0, int N, float scale, float4* pos4) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= N) return;
+  int a = orig[s];
+  pos4[s] = pack_delta(pos0[a], R[3 * a] - R0[3 * a], R[3 * a + 1] - R0[3 * a + 1], R[3 * a + 2] - R0[3 * a + 2],
+                       scale);
 }
 
 // scaled FP64 coordinates Rs = R/L (src/EmDeeCode.f90:1228) in slot order
@@ -323,8 +343,11 @@ void device_pack(System& s) {
   prof_begin(s, PK_PACK);
   if (s.precision == 1) {
     k_pack_fp64<<<bl, th, 0, s.stream>>>(s.dR, g.dOrig, N, *s.Lbox, g.dRs64);
-  } else {
-    k_pack_mixed<<<bl, th, 0, s.stream>>>(s.dR, s.dCharge, g.dOrig, g.dK, N, (double)g.M / *s.Lbox, g.dPos4);
+  } else if (*s.Lbox == s.builtL) {
+    k_pack_delta<<<bl, th, 0, s.stream>>>(s.dR, s.dR0, g.dOrig, g.dPos0, N, (float)((double)g.M / *s.Lbox), g.dPos4);
+  } else {   // the box changed since the build: from the coordinates
+    k_pack_mixed<<<bl, th, 0, s.stream>>>(s.dR, s.dCharge, g.dOrig, g.dK, N, (double)g.M / *s.Lbox, g.dPos4,
+                                          (float4*)nullptr);
   }
   CK(cudaGetLastError());
   prof_end(s, PK_PACK);
@@ -554,11 +577,11 @@ void device_build_lists(System& s) {
       CK(cudaFree(g.dType8)); CK(cudaFree(g.dRs64)); CK(cudaFree(g.dNbCount)); CK(cudaFree(g.dNbInner));
       CK(cudaFree(g.dSelf));
       CK(cudaFree(g.dSlotOf));
-      CK(cudaFree(g.dAtomKd));
+      CK(cudaFree(g.dPos0));
       CK(cudaFree(g.dKeyX));
       CK(cudaMalloc(&g.dKeyX, sizeof(float) * N));
       CK(cudaMalloc(&g.dSlotOf, sizeof(int) * N));
-      CK(cudaMalloc(&g.dAtomKd, sizeof(double) * 3 * N));
+      CK(cudaMalloc(&g.dPos0, sizeof(float4) * N));
       CK(cudaMalloc(&g.dOrig, sizeof(int) * N));
       CK(cudaMalloc(&g.dK, sizeof(int4) * N));
       CK(cudaMalloc(&g.dAtomK, sizeof(int4) * N));
@@ -579,7 +602,7 @@ void device_build_lists(System& s) {
     CK(cudaMemsetAsync(g.dCount, 0, sizeof(int) * (g.nRanks + 1), s.stream));
     s.prof.total += 8;   // assign, 3 scan phases, scatter, sort, fill, tile info
     // the slot array holds each atom's place in its cell until k_fill_slots
-    k_assign<<<bl, th, 0, s.stream>>>(s.dR, N, 1.0 / L, geo, g.dAtomK, g.dAtomKd, g.dCount, g.dSlotOf);
+    k_assign<<<bl, th, 0, s.stream>>>(s.dR, N, 1.0 / L, geo, g.dAtomK, g.dCount, g.dSlotOf);
     CK(cudaGetLastError());
     device_scan(s, g.dCount, g.dStart, g.nRanks);
     k_scatter<<<bl, th, 0, s.stream>>>(g.dAtomK, N, g.dStart, g.dSlotOf, g.dOrig);
@@ -663,7 +686,7 @@ void device_build_lists(System& s) {
   // positions for the FP32 prefilter
   {
     int th = 256, bl = (N + th - 1) / th;
-    k_pack_mixed<<<bl, th, 0, s.stream>>>(s.dR, s.dCharge, g.dOrig, g.dK, N, (double)g.M / L, g.dPos4);
+    k_pack_mixed<<<bl, th, 0, s.stream>>>(s.dR, s.dCharge, g.dOrig, g.dK, N, (double)g.M / L, g.dPos4, g.dPos0);
     CK(cudaGetLastError());
     s.prof.total++;
   }
@@ -902,8 +925,7 @@ __global__ void __launch_bounds__(SKIN_THREADS) k_step_fused(double* __restrict_
                                                              const double* __restrict__ R0, int N, double cf0,
                                                              double cf1, double CP, double skinSq,
                                                              const int* __restrict__ slotOf,
-                                                             const double* __restrict__ atomKd,
-                                                             const double* __restrict__ charge, double scale,
+                                                             const float4* __restrict__ pos0, float scale,
                                                              float4* __restrict__ pos4, longlong2* partial,
                                                              unsigned int* ticket, double* result) {
   __shared__ MaxPrev wsum[SKIN_THREADS / 32];
@@ -933,13 +955,7 @@ __global__ void __launch_bounds__(SKIN_THREADS) k_step_fused(double* __restrict_
       }
       const double d0 = r[0] - R0[3 * i], d1 = r[1] - R0[3 * i + 1], d2 = r[2] - R0[3 * i + 2];
       v.m = __double_as_longlong(FMA ? fma(d2, d2, fma(d1, d1, d0 * d0)) : d0 * d0 + d1 * d1 + d2 * d2);
-      if (PACK) {
-        const double q = charge[i];
-        float u[3];
-        for (int d = 0; d < 3; d++)
-          u[d] = (float)(FMA ? fma(r[d], scale, -atomKd[3 * i + d]) : r[d] * scale - atomKd[3 * i + d]);
-        pos4[slotOf[i]] = make_float4(u[0], u[1], u[2], fabs(q) > 2.220446049250313e-16 ? (float)q : 0.0f);
-      }
+      if (PACK) pos4[slotOf[i]] = pack_delta(pos0[i], d0, d1, d2, scale);
     }
     v = warp_ordered_combine(v);
     run = mp_combine(run, v);
@@ -983,12 +999,12 @@ void device_step_fused(System& s, double CP) {
   const int N = s.natoms;
   const int blocks = (N + SKIN_THREADS * STEP_CHUNKS - 1) / (SKIN_THREADS * STEP_CHUNKS);
   ensure_partials(s, blocks);
-  const bool pack = s.precision == 0 && s.r0Valid;
+  const bool pack = s.precision == 0 && s.r0Valid && *s.Lbox == s.builtL;
   const Grid& g = s.grid;
-  const double scale = g.M > 0 ? (double)g.M / *s.Lbox : 0.0;
+  const float scale = g.M > 0 ? (float)((double)g.M / *s.Lbox) : 0.0f;
   prof_begin(s, PK_MOVE);
 #define STEP_ARGS s.dR, s.dP, s.F(), s.dInvMass, s.dR0, N, s.pendCF[0], s.pendCF[1], CP, s.skinSq, g.dSlotOf, \
-                  g.dAtomKd, s.dCharge, scale, g.dPos4, (longlong2*)s.dPartials, s.dTicket, s.dResult
+                  g.dPos0, scale, g.dPos4, (longlong2*)s.dPartials, s.dTicket, s.dResult
 #define STEP_LAUNCH(NK, UM, PK, FM) k_step_fused<NK, UM, PK, FM><<<blocks, SKIN_THREADS, 0, s.stream>>>(STEP_ARGS)
 #define STEP_NK(UM, PK, FM)                 \
   if (s.npend == 0) STEP_LAUNCH(0, UM, PK, FM); \

@@ -136,7 +136,7 @@ struct Grid {
   int4* dK = nullptr;
   int4* dAtomK = nullptr;
   int* dSlotOf = nullptr;   // atom -> slot of the last build
-  double* dAtomKd = nullptr;   // the build-time unwrapped cell of each atom, as doubles
+  float4* dPos0 = nullptr;     // per atom: packed position (u, charge) at the last build
   float* dKeyX = nullptr;      // sort key of each slot (cell-local x) during a build
   float4* dPos4 = nullptr;
   uint8_t* dType8 = nullptr;
