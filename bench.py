@@ -142,9 +142,9 @@ def fp32_peak_tflops(torch):
     return best
 
 
-def read_traffic():
-    """DRAM bytes per pair-kernel launch from the committed ncu summary, if any."""
-    p = os.path.join(ROOT, "profiles", "pair_lj1m_traffic.txt")
+def read_traffic(name="pair_lj1m_traffic.txt"):
+    """DRAM bytes per kernel launch from a committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", name)
     try:
         for line in open(p):
             if line.startswith("dram_bytes_per_launch"):
@@ -269,14 +269,15 @@ def run_gpu(args):
                 "us_per_launch": pair_s * 1e6}
     boost_bytes = 72.0 * N   # P read+write, F read (steps with energies only)
     # fused step (two deferred kicks + move + skin displacement + FP32 packing), unit masses:
-    # P r/w 48, F 24, R r/w 48, R0 24, build-time cell 16, slot 4, charge 8, packed position 16
-    move_bytes = 188.0 * N
+    # P r/w 48, F 24, R r/w 48, R0 24, build-time position and charge 16, slot 4, packed position 16
+    move_bytes = 172.0 * N
     hbm = peaks.get("hbm_gbs", 6800.0)
     boost_gbs = boost_bytes / (kms[4] / kn[4] * 1e-3) / 1e9 if kn[4] else None
     move_gbs = move_bytes / (kms[5] / kn[5] * 1e-3) / 1e9 if kn[5] else None
     roofline_hbm = {"bound": "hbm", "kernel": "k_step_fused (EmDee_displace: deferred boosts, move, skin, pack)",
                     "achieved": move_gbs, "peak": hbm,
-                    "unit": "GB/s", "frac": (move_gbs / hbm) if move_gbs else None, "traffic": None,
+                    "unit": "GB/s", "frac": (move_gbs / hbm) if move_gbs else None,
+                    "traffic": read_traffic("step_fused_lj1m_traffic.txt"), "bytes_per_launch": move_bytes,
                     "peak_source": peak_kind, "boost_achieved_gbs": boost_gbs}
 
     # whole step against both ceilings: max(FLOPs / FP32 peak, bytes / HBM peak) per step
