@@ -197,6 +197,25 @@ def run_reference(args):
 # GPU arm
 # ---------------------------------------------------------------------------------
 
+def max_over_ranks(x, world, device):
+    """The largest value of x over the ranks of the job (x itself for one rank): the
+    slowest rank's time defines the whole job's time."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_rank, ms, world, device):
+    """Whole-job throughput: the units all ranks processed over the slowest rank's time.
+    Returns (rate per second, slowest time in ms)."""
+    ms_max = max_over_ranks(ms, world, device)
+    return world * units_per_rank / (ms_max * 1e-3), ms_max
+
+
 def run_gpu(args):
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -237,11 +256,7 @@ def run_gpu(args):
     ms = e0.elapsed_time(e1)
     launches = lib.EmDee_launch_count(md) - launches0
     builds = md.Builds - builds0
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * N * args.steps / (ms * 1e-3)
+    value, ms = job_rate(N * args.steps, ms, world, "cuda")
 
     # ---- per-kernel device times (same workload, CUDA events on the library stream) ----
     lib.EmDee_profile(md, 1)
@@ -309,8 +324,8 @@ def run_gpu(args):
     f1.record(stream)
     f1.synchronize()
     barrier()
-    e2e_ms = f0.elapsed_time(f1)
-    e2e = {"value": world * N * ne2e / (e2e_ms * 1e-3), "unit": "atom-steps/s", "h2d_bytes_per_step": 24 * N,
+    e2e_rate, e2e_ms = job_rate(N * ne2e, f0.elapsed_time(f1), world, "cuda")
+    e2e = {"value": e2e_rate, "unit": "atom-steps/s", "h2d_bytes_per_step": 24 * N,
            "d2h_bytes_per_step": 48 * N + 40, "steps": ne2e,
            "per_step": "EmDee_upload(momenta) from pinned host memory, boost/displace/boost, "
                        "EmDee_download(coordinates) and EmDee_download(momenta) into pinned host memory"}
