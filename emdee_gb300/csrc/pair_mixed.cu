@@ -21,11 +21,15 @@
 namespace emdee {
 
 static const int PAIR_THREADS = 256;   // upper bound; launches use one thread per tile atom
+// The general variant (VAR 1) may run several threads per atom in blocks of up to
+// PAIR_THREADS_GENERAL threads.
+static const int PAIR_THREADS_GENERAL = 1024;
+#define PAIR_MAX_THREADS (VAR == 1 ? PAIR_THREADS_GENERAL : PAIR_THREADS)
 // PAIR_MIN_BLOCKS (compile-time): resident blocks per SM the register budget must allow
 #ifdef PAIR_MIN_BLOCKS
-#define PAIR_BOUNDS __launch_bounds__(PAIR_THREADS, PAIR_MIN_BLOCKS)
+#define PAIR_BOUNDS __launch_bounds__(PAIR_MAX_THREADS, PAIR_MIN_BLOCKS)
 #else
-#define PAIR_BOUNDS __launch_bounds__(PAIR_THREADS)
+#define PAIR_BOUNDS __launch_bounds__(PAIR_MAX_THREADS)
 #endif
 
 struct PairArgsF {
@@ -39,6 +43,7 @@ struct PairArgsF {
   const uint16_t* nb;
   const int* count;
   int cap, tileStride, haloCap;
+  int tpa, tpaShift;   // threads per atom (a power of 2, at most 8) and its log2
   const PairEntry<float>* table;   // this layer: [itype][jtype] -> pair(jtype, itype)
   const NBParams<float>* coul;
   int ntypes;
@@ -89,7 +94,11 @@ __global__ void PAIR_BOUNDS k_pair_mixed(PairArgsF A) {
   const int tb = A.start[t * cells], te = A.start[(t + 1) * cells];
   const int capC = A.cap >> 3;
   float Ep = 0.f, Ec = 0.f, Wp = 0.f, Wc = 0.f, within = 0.f;
-  for (int li = threadIdx.x; li < te - tb; li += blockDim.x) {
+  // tpa consecutive threads share an atom: thread sub takes the chunks sub, sub + tpa, ...
+  // and the group's partial forces are summed by shuffles in a fixed order
+  const int tpa = VAR == 1 ? A.tpa : 1, tpaShift = VAR == 1 ? A.tpaShift : 0, sub = threadIdx.x & (tpa - 1);
+  const unsigned gmask = (0xFFFFFFFFu >> (32 - tpa)) << ((threadIdx.x & 31) & ~(tpa - 1));
+  for (int li = threadIdx.x >> tpaShift; li < te - tb; li += blockDim.x >> tpaShift) {
     const int si = tb + li;
     const int qi = A.self[si];
     const float4 pi = hpos[qi];
@@ -98,9 +107,9 @@ __global__ void PAIR_BOUNDS k_pair_mixed(PairArgsF A) {
     const uint4* lp = reinterpret_cast<const uint4*>(A.nb) + ((size_t)t * capC * A.tileStride + li);
     const int ti = VAR == 1 ? htype[qi] : 0;
     float fx = 0.f, fy = 0.f, fz = 0.f;
-    uint4 cur = nch > 0 ? __ldcs(lp) : make_uint4(0u, 0u, 0u, 0u);
-    for (int c = 0; c < nch; c++) {
-      const uint4 nxt = (c + 1 < nch) ? __ldcs(lp + (size_t)(c + 1) * A.tileStride) : cur;
+    uint4 cur = sub < nch ? __ldcs(lp + (size_t)sub * A.tileStride) : make_uint4(0u, 0u, 0u, 0u);
+    for (int c = sub; c < nch; c += tpa) {
+      const uint4 nxt = (c + tpa < nch) ? __ldcs(lp + (size_t)(c + tpa) * A.tileStride) : cur;
       const unsigned w[4] = {cur.x, cur.y, cur.z, cur.w};
 #pragma unroll
       for (int e = 0; e < 8; e++) {
@@ -153,7 +162,12 @@ __global__ void PAIR_BOUNDS k_pair_mixed(PairArgsF A) {
       }
       cur = nxt;
     }
-    if (!COUNT) {
+    for (int o = tpa >> 1; o > 0; o >>= 1) {
+      fx += __shfl_xor_sync(gmask, fx, o);
+      fy += __shfl_xor_sync(gmask, fy, o);
+      fz += __shfl_xor_sync(gmask, fz, o);
+    }
+    if (!COUNT && sub == 0) {
       double* Fa = A.F + 3 * (size_t)A.orig[si];
       Fa[0] = f2d_exact(fx * A.invw);
       Fa[1] = f2d_exact(fy * A.invw);
@@ -165,7 +179,7 @@ __global__ void PAIR_BOUNDS k_pair_mixed(PairArgsF A) {
   // without COUNT) skip the reduction.
   const float v[5] = {0.5f * Ep, 0.5f * Ec, 0.5f * Wp, 0.5f * Wc, 0.5f * within};
   constexpr unsigned MASK = (COMPUTE ? (VAR == 1 ? 3u : 1u) : 0u) | (VAR == 1 ? 12u : 4u) | (COUNT ? 16u : 0u);
-  grid_reduce_ff<5, PAIR_THREADS, MASK>(v, reinterpret_cast<float2*>(A.partials), A.ticket, A.result);
+  grid_reduce_ff<5, PAIR_MAX_THREADS, MASK>(v, reinterpret_cast<float2*>(A.partials), A.ticket, A.result);
 }
 
 template <bool COMPUTE, int VAR, int MOD, bool MINIMG, bool COUNT>
@@ -226,11 +240,25 @@ void device_pair_forces_mixed(System& s, bool compute, bool useInRc, double rc2s
   size_t smem = (size_t)(g.maxHalo + 1) * sizeof(float4) + sizeof(int) * (3 * g.haloCells + 1);
   if (variant != 0) smem += sizeof(PairEntry<float>) * s.ntypes * s.ntypes + g.maxHalo + 17;
   const bool mi = g.M == 5;
-  // threads per block: one per tile atom up to the tile's largest count, or
-  // fewer with several atoms per thread (EMDEE_PAIR_THREADS, a multiple of 32)
+  // Threads per atom: systems too small to fill the GPU with one thread per atom
+  // (fewer than ~2048 threads per SM) and with long lists (more than 48 entries per
+  // thread) split each list over 2, 4 or 8 threads of a warp (general variant only,
+  // blocks of up to 1024 threads).  Threads per block: the tile's largest atom count
+  // times that, or fewer with several atoms per thread (EMDEE_PAIR_THREADS).
+  const int maxTh = variant == 0 ? PAIR_THREADS : PAIR_THREADS_GENERAL;
+  const double L3 = L * L * L, expected = s.natoms / L3 * 4.18879020478639 * s.xRcSq * s.xRc;
+  int tpa = 1, shift = 0;
+  if (variant != 0)
+    while (tpa < 8 && g.tileStride * tpa * 2 <= maxTh && (double)s.natoms * tpa * 2 <= 152.0 * 2048 &&
+           expected / (tpa * 2) >= 48) {
+      tpa *= 2;
+      shift++;
+    }
+  A.tpa = tpa;
+  A.tpaShift = shift;
   static const int thEnv = getenv("EMDEE_PAIR_THREADS") ? atoi(getenv("EMDEE_PAIR_THREADS")) : 0;
-  const int th = thEnv >= 32 && thEnv % 32 == 0 ? std::min(thEnv, PAIR_THREADS)
-                                                 : std::min(PAIR_THREADS, std::max(32, g.tileStride));
+  const int th = thEnv >= 32 && thEnv % 32 == 0 ? std::min(thEnv, maxTh)
+                                                 : std::min(maxTh, std::max(32, g.tileStride * tpa));
   const int nt = g.nTiles;
   if (variant == 0) {
     const int mod = s.P(0, 0, s.layer - 1).model.p.modifier;
