@@ -64,6 +64,7 @@ void prof_begin(System& s, int kind) {
   (void)kind;
   s.prof.total++;
   if (!s.prof.on) return;
+  if (s.prof.kind.size() >= 4096) prof_resolve(s);
   cudaEvent_t e = prof_event(s);
   CK(cudaEventRecord(e, s.stream));
   s.prof.ev.push_back(e);
@@ -75,7 +76,17 @@ void prof_end(System& s, int kind) {
   CK(cudaEventRecord(e, s.stream));
   s.prof.ev.push_back(e);
   s.prof.kind.push_back(kind);
-  if (s.prof.kind.size() >= 4096) prof_resolve(s);
+}
+
+// forgets the timing of the last begin/end pair (a launch that returned at once;
+// it still counts as a launch)
+void prof_drop_last(System& s) {
+  if (!s.prof.on || s.prof.kind.empty()) return;
+  s.prof.kind.pop_back();
+  for (int k = 0; k < 2; k++) {
+    s.prof.pool.push_back(s.prof.ev.back());
+    s.prof.ev.pop_back();
+  }
 }
 
 static double wtime() {
@@ -285,19 +296,30 @@ static void compute_forces_impl(tEmDee* md) {
   bool compute = md->Options.Compute;
   double t0 = wtime();
   flush_pending(s);   // deferred boosts use the forces they were issued with
-  bool rebuild = !s.r0Valid;
-  if (!rebuild) rebuild = s.skinReady ? device_skin_from_step(s) : device_skin_check(s);
-  else s.hResult[9] = 1.0;
+  bool rebuild = !s.r0Valid, forcesDone = false;
+  if (!rebuild && s.skinReady && s.packReady && s.precision == 0 && s.pairs_exist[s.layer - 1]) {
+    // the fused step left the skin decision and the packed positions on the device:
+    // the pair kernel runs unless a rebuild is due, and one synchronisation returns
+    // both the decision and the sums
+    forcesDone = device_pair_forces(s, compute, true);
+    rebuild = !forcesDone;
+  } else if (!rebuild) {
+    rebuild = s.skinReady ? device_skin_from_step(s) : device_skin_check(s);
+  } else {
+    s.hResult[9] = 1.0;
+  }
   if (rebuild) {
     device_build_lists(s);
     md->Builds++;
   }
   double t1 = wtime();
   md->Time.Neighbor += t1 - t0;
-  // the build packs the FP32 positions for its prefilter; a fused step packs them too
-  if (!((rebuild || s.packReady) && s.precision == 0)) device_pack(s);
+  if (!forcesDone) {
+    // the build packs the FP32 positions for its prefilter; a fused step packs them too
+    if (!((rebuild || s.packReady) && s.precision == 0)) device_pack(s);
+    device_pair_forces(s, compute);
+  }
   s.skinReady = s.packReady = false;
-  device_pair_forces(s, compute);
   const double* r = s.hResult;   // Epair, Ecoul, Wpair, Wcoul
   double bonded[5];   // Ebond, Wbond, Eangle, Wangle, Coulomb discounts of bonds and angles
   device_bonded(s, bonded);

@@ -147,7 +147,7 @@ void flush_pending(System& s) {
 
 // Chooses the force kernel for the current layer and leaves the four sums in
 // hResult[0..3] (src/EmDeeData.f90:644-685).
-void device_pair_forces(System& s, bool compute) {
+bool device_pair_forces(System& s, bool compute, bool speculative) {
   const int l = s.layer - 1;
   const double L = *s.Lbox, invL2 = 1.0 / (L * L);
   const bool useInRc = s.useInRc[l] != 0;
@@ -156,7 +156,7 @@ void device_pair_forces(System& s, bool compute) {
     CK(cudaMemsetAsync(s.F(), 0, sizeof(double) * 3 * s.natoms, s.stream));
     CK(cudaStreamSynchronize(s.stream));
     for (int q = 0; q < 4; q++) s.hResult[q] = 0.0;
-    return;
+    return true;
   }
   if (s.partialCap < s.grid.nTiles) {
     CK(cudaFree(s.dPartials));
@@ -170,11 +170,20 @@ void device_pair_forces(System& s, bool compute) {
     // single-type Lennard-Jones without charges takes the specialised kernel
     bool lj_only = s.ntypes == 1 && s.P(0, 0, l).model.kind == MK_LJ_CUT &&
                    !(s.P(0, 0, l).coulomb && s.coul[l].kind != MK_COUL_NONE);
+    s.pairSkip = speculative ? s.dResult + 9 : nullptr;
     device_pair_forces_mixed(s, compute, useInRc, rc2, lj_only ? 0 : 1);
+    s.pairSkip = nullptr;
   }
   prof_end(s, PK_PAIR);
-  CK(cudaMemcpyAsync(s.hResult, s.dResult, 4 * sizeof(double), cudaMemcpyDeviceToHost, s.stream));
+  // speculative: the skin value and rebuild flag ([8], [9]) come back with the sums
+  CK(cudaMemcpyAsync(s.hResult, s.dResult, (speculative ? 10 : 4) * sizeof(double), cudaMemcpyDeviceToHost,
+                     s.stream));
   CK(cudaStreamSynchronize(s.stream));
+  if (speculative && s.hResult[9] != 0.0) {
+    prof_drop_last(s);
+    return false;
+  }
+  return true;
 }
 
 // Half-list statistics: entries of the current lists and pairs within the

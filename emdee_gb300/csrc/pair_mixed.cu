@@ -52,6 +52,7 @@ struct PairArgsF {
   float invw;
   float Mf;
   double* F;     // forces, API order, double[N][3]
+  const double* skip;   // if set and *skip != 0 (a rebuild is due), the launch does nothing
   double* partials;
   unsigned int* ticket;
   double* result;
@@ -66,6 +67,7 @@ struct PairArgsF {
 // wrap would bring the sentinel back).
 template <bool COMPUTE, int VAR, int MOD, bool MINIMG, bool COUNT>
 __global__ void PAIR_BOUNDS k_pair_mixed(PairArgsF A) {
+  if (A.skip != nullptr && *A.skip != 0.0) return;
   extern __shared__ __align__(16) unsigned char sraw[];
   __shared__ int ws[33];
   const TileGeom g = A.g;
@@ -234,6 +236,7 @@ void device_pair_forces_mixed(System& s, bool compute, bool useInRc, double rc2s
   A.invw = (float)(1.0 / w);
   A.Mf = (float)g.M;
   A.F = s.F();
+  A.skip = s.pairSkip;
   A.partials = s.dPartials;
   A.ticket = s.dTicket;
   A.result = s.dResult;

@@ -229,6 +229,7 @@ struct System {
   double pendCF[2] = {0.0, 0.0};
   bool skinReady = false, packReady = false;
   bool phaseShared = false;   // R/P aliased with another system (no deferral then)
+  const double* pairSkip = nullptr;   // device rebuild flag the mixed pair kernel checks first
   double builtL = 0;           // box length at the last build
 
   // reduction scratch
@@ -260,6 +261,7 @@ struct System {
 System* sys_of(const tEmDee& md);
 void prof_begin(System& s, int kind);
 void prof_end(System& s, int kind);
+void prof_drop_last(System& s);
 
 // ---- device entry points (neighbor.cu, pair_*.cu, motion.cu) ---------------------
 
@@ -272,7 +274,10 @@ void device_build_lists(System& s);
 void device_pack(System& s);
 // Pair forces, energies and virials of the current layer into s.F();
 // leaves Epair, Ecoul, Wpair, Wcoul in hResult after synchronizing.
-void device_pair_forces(System& s, bool compute);
+// Forces of the current layer; energies and virials in hResult[0..3].  speculative
+// (mixed precision, after a fused step): the kernel runs only if the step's skin
+// check found no rebuild due; returns false if it did not run.
+bool device_pair_forces(System& s, bool compute, bool speculative = false);
 // P <- CP P + CF F (free atoms); optional 2KE per dimension into hResult[10..12].
 void device_boost(System& s, double CP, double CF, bool kinetic);
 void device_kinetic(System& s, double* twoKE);   // free atoms only (no bodies)
