@@ -444,7 +444,16 @@ __global__ void BUILD_BOUNDS k_build(BuildArgs A) {
   uint8_t* sinter = (uint8_t*)(hxyz + g.haloCells);
   uint8_t* htype = sinter + A.ntypes * A.ntypes;
   for (int k = threadIdx.x; k < A.ntypes * A.ntypes; k += blockDim.x) sinter[k] = A.interact[k];
-  halo_layout(g, t, A.tab, A.start, off, cst, hxyz, ws);
+  const int haloCount = halo_layout(g, t, A.tab, A.start, off, cst, hxyz, ws);
+  {
+    // sizes taken from the previous build: a tile or halo that outgrew them is
+    // reported (the host re-sizes and builds again) before anything is staged
+    const int tileCount = A.start[(t + 1) * g.TB * g.TB * g.TB] - A.start[t * g.TB * g.TB * g.TB];
+    if (tileCount > A.tileStride || haloCount > A.haloCap) {
+      if (threadIdx.x == 0) atomicOr(A.maxCount + 1, 1);
+      return;
+    }
+  }
   stage_frame(g, off, cst, hxyz, A.pos4, hpos, hslot, single ? (uint8_t*)nullptr : htype, A.type8);
   __syncthreads();
   const bool none = A.ntypes == 1 && !sinter[0];   // the only type pair does not interact: empty lists
@@ -544,17 +553,19 @@ static int choose_tile(int M, double perCell) {
   return std::min(tb, M);
 }
 
-// src/neighbor_lists.f90:175-195 (build part) and 199-300
-void device_build_lists(System& s) {
+// src/neighbor_lists.f90:175-195 (build part) and 199-300.  reuse: keep the tile
+// sizes of the previous build when the cell geometry is unchanged (no per-tile
+// count pass and no synchronisation for it); returns false if a tile outgrew them.
+static bool build_lists(System& s, bool reuse) {
   Grid& g = s.grid;
   GridCaps& c = g.caps;
   const int N = s.natoms;
-  prof_begin(s, PK_BUILD);
   const double L = *s.Lbox;
   int M = (int)std::floor(NDIV * L / s.xRc);
   M = std::max(M, 2 * NDIV + 1);
   double perCell = (double)N / ((double)M * M * M);
   int TB = choose_tile(M, perCell);
+  reuse = reuse && g.M == M && g.TB == TB && g.maxHalo > 0 && g.tileStride > 0 && c.atoms >= (size_t)N;
   size_t smemLimit = 200 * 1024;
   for (;;) {
     TileGeom geo = make_geom(M, TB);
@@ -600,7 +611,7 @@ void device_build_lists(System& s) {
     }
     int th = 256, bl = (N + th - 1) / th;
     CK(cudaMemsetAsync(g.dCount, 0, sizeof(int) * (g.nRanks + 1), s.stream));
-    s.prof.total += 8;   // assign, 3 scan phases, scatter, sort, fill, tile info
+    s.prof.total += reuse ? 7 : 8;   // assign, 3 scan phases, scatter, sort, fill (, tile info)
     // the slot array holds each atom's place in its cell until k_fill_slots
     k_assign<<<bl, th, 0, s.stream>>>(s.dR, N, 1.0 / L, geo, g.dAtomK, g.dCount, g.dSlotOf);
     CK(cudaGetLastError());
@@ -611,6 +622,7 @@ void device_build_lists(System& s) {
     k_fill_slots<<<bl, th, 0, s.stream>>>(g.dOrig, N, g.dAtomK, s.dType, g.dK, g.dType8, g.dSlotOf);
     int* dMax = g.dTileInfo + 2 * g.nTiles;
     CK(cudaMemsetAsync(dMax, 0, sizeof(int) * 4, s.stream));
+    if (reuse) break;
     k_tile_info<<<g.nTiles, 128, 0, s.stream>>>(g.dStart, geo, g.dTileInfo, dMax);
     CK(cudaGetLastError());
     int hmax[2];
@@ -707,17 +719,24 @@ void device_build_lists(System& s) {
     kb<<<g.nTiles, std::min(BUILD_THREADS, std::max(32, g.tileStride)), smem, s.stream>>>(A);
     s.prof.total++;
     CK(cudaGetLastError());
-    int mc = 0;
-    CK(cudaMemcpyAsync(&mc, A.maxCount, sizeof(int), cudaMemcpyDeviceToHost, s.stream));
+    int mc[2] = {0, 0};   // largest list, tile-size overflow
+    CK(cudaMemcpyAsync(mc, A.maxCount, 2 * sizeof(int), cudaMemcpyDeviceToHost, s.stream));
     CK(cudaStreamSynchronize(s.stream));
-    if (mc <= g.cap) break;
-    if (mc > 65528) fatal("neighbor list build", "more than 65528 neighbors for one atom");
-    g.cap = std::min(65528, (mc + mc / 8 + 16 + 7) / 8 * 8);
+    if (mc[1]) return false;
+    if (mc[0] <= g.cap) break;
+    if (mc[0] > 65528) fatal("neighbor list build", "more than 65528 neighbors for one atom");
+    g.cap = std::min(65528, (mc[0] + mc[0] / 8 + 16 + 7) / 8 * 8);
   }
   CK(cudaMemcpyAsync(s.dR0, s.dR, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, s.stream));
-  prof_end(s, PK_BUILD);
   s.r0Valid = true;
   s.builtL = L;
+  return true;
+}
+
+void device_build_lists(System& s) {
+  prof_begin(s, PK_BUILD);
+  if (!build_lists(s, true)) build_lists(s, false);
+  prof_end(s, PK_BUILD);
 }
 
 // ---------------------------------------------------------------------------------
