@@ -250,14 +250,25 @@ __global__ void k_sort_cells(const int* start, int nRanks, int* orig, const doub
   }
 }
 
+// per slot: image cell, type, slot of the atom, and the FP32 position and charge
+// (k_pack_mixed's values, also kept per atom as the build-time reference)
 __global__ void k_fill_slots(const int* orig, int N, const int4* atomK, const int* type, int4* K, uint8_t* type8,
-                             int* slotOf) {
+                             int* slotOf, const double* __restrict__ R, const double* __restrict__ charge,
+                             double scale, float4* pos4, float4* pos0) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= N) return;
   int a = orig[s];
-  K[s] = atomK[a];
+  const int4 k = atomK[a];
+  K[s] = k;
   slotOf[a] = s;
   type8[s] = (uint8_t)(type[a] - 1);
+  float ux = (float)(R[3 * a] * scale - (double)k.x);
+  float uy = (float)(R[3 * a + 1] * scale - (double)k.y);
+  float uz = (float)(R[3 * a + 2] * scale - (double)k.z);
+  double q = charge[a];
+  const float4 v = make_float4(ux, uy, uz, fabs(q) > 2.220446049250313e-16 ? (float)q : 0.0f);
+  pos4[s] = v;
+  pos0[a] = v;
 }
 
 __global__ void k_halo_table(TileGeom g, int2* tab) {
@@ -619,7 +630,8 @@ static bool build_lists(System& s, bool reuse) {
     k_scatter<<<bl, th, 0, s.stream>>>(g.dAtomK, N, g.dStart, g.dSlotOf, g.dOrig);
     k_sort_cells<<<(g.nRanks + 255) / 256, 256, 0, s.stream>>>(g.dStart, g.nRanks, g.dOrig, s.dR, g.dAtomK,
                                                                (double)M / L, g.dKeyX);
-    k_fill_slots<<<bl, th, 0, s.stream>>>(g.dOrig, N, g.dAtomK, s.dType, g.dK, g.dType8, g.dSlotOf);
+    k_fill_slots<<<bl, th, 0, s.stream>>>(g.dOrig, N, g.dAtomK, s.dType, g.dK, g.dType8, g.dSlotOf, s.dR,
+                                          s.dCharge, (double)M / L, g.dPos4, g.dPos0);
     int* dMax = g.dTileInfo + 2 * g.nTiles;
     CK(cudaMemsetAsync(dMax, 0, sizeof(int) * 4, s.stream));
     if (reuse) break;
@@ -695,13 +707,6 @@ static bool build_lists(System& s, bool reuse) {
   A.selfIdx = g.dSelf;
   A.tileStride = g.tileStride;
   A.maxCount = g.dTileInfo + 2 * g.nTiles + 2;
-  // positions for the FP32 prefilter
-  {
-    int th = 256, bl = (N + th - 1) / th;
-    k_pack_mixed<<<bl, th, 0, s.stream>>>(s.dR, s.dCharge, g.dOrig, g.dK, N, (double)g.M / L, g.dPos4, g.dPos0);
-    CK(cudaGetLastError());
-    s.prof.total++;
-  }
   size_t smem = build_smem(g, s.ntypes);
   const bool general = s.ntypes > 1 || A.hasBodies || A.hasEx || A.layered;
   auto kb = general ? (A.minimg ? k_build<true, true> : k_build<true, false>)
