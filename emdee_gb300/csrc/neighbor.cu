@@ -254,7 +254,7 @@ __global__ void k_sort_cells(const int* start, int nRanks, int* orig, const doub
 // (k_pack_mixed's values, also kept per atom as the build-time reference)
 __global__ void k_fill_slots(const int* orig, int N, const int4* atomK, const int* type, int4* K, uint8_t* type8,
                              int* slotOf, const double* __restrict__ R, const double* __restrict__ charge,
-                             double scale, float4* pos4, float4* pos0) {
+                             double scale, float4* pos4, float4* pos0, double* __restrict__ R0) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= N) return;
   int a = orig[s];
@@ -262,13 +262,17 @@ __global__ void k_fill_slots(const int* orig, int N, const int4* atomK, const in
   K[s] = k;
   slotOf[a] = s;
   type8[s] = (uint8_t)(type[a] - 1);
-  float ux = (float)(R[3 * a] * scale - (double)k.x);
-  float uy = (float)(R[3 * a + 1] * scale - (double)k.y);
-  float uz = (float)(R[3 * a + 2] * scale - (double)k.z);
+  const double rx = R[3 * a], ry = R[3 * a + 1], rz = R[3 * a + 2];
+  float ux = (float)(rx * scale - (double)k.x);
+  float uy = (float)(ry * scale - (double)k.y);
+  float uz = (float)(rz * scale - (double)k.z);
   double q = charge[a];
   const float4 v = make_float4(ux, uy, uz, fabs(q) > 2.220446049250313e-16 ? (float)q : 0.0f);
   pos4[s] = v;
   pos0[a] = v;
+  R0[3 * a] = rx;   // the positions of this build, for the skin check
+  R0[3 * a + 1] = ry;
+  R0[3 * a + 2] = rz;
 }
 
 __global__ void k_halo_table(TileGeom g, int2* tab) {
@@ -631,7 +635,7 @@ static bool build_lists(System& s, bool reuse) {
     k_sort_cells<<<(g.nRanks + 255) / 256, 256, 0, s.stream>>>(g.dStart, g.nRanks, g.dOrig, s.dR, g.dAtomK,
                                                                (double)M / L, g.dKeyX);
     k_fill_slots<<<bl, th, 0, s.stream>>>(g.dOrig, N, g.dAtomK, s.dType, g.dK, g.dType8, g.dSlotOf, s.dR,
-                                          s.dCharge, (double)M / L, g.dPos4, g.dPos0);
+                                          s.dCharge, (double)M / L, g.dPos4, g.dPos0, s.dR0);
     int* dMax = g.dTileInfo + 2 * g.nTiles;
     CK(cudaMemsetAsync(dMax, 0, sizeof(int) * 4, s.stream));
     if (reuse) break;
@@ -732,8 +736,7 @@ static bool build_lists(System& s, bool reuse) {
     if (mc[0] > 65528) fatal("neighbor list build", "more than 65528 neighbors for one atom");
     g.cap = std::min(65528, (mc[0] + mc[0] / 8 + 16 + 7) / 8 * 8);
   }
-  CK(cudaMemcpyAsync(s.dR0, s.dR, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, s.stream));
-  s.r0Valid = true;
+  s.r0Valid = true;   // R0 was written by k_fill_slots
   s.builtL = L;
   return true;
 }
