@@ -225,7 +225,7 @@ __global__ void k_scatter(const int4* atomK, int N, const int* start, const int*
 }
 
 // Order inside a cell: ascending cell-local x coordinate u.x (computed as in
-// k_pack_mixed, so the build's staged positions are sorted along x within
+// k_fill_slots, so the build's staged positions are sorted along x within
 // every cell and hence along every stencil row), ties by ascending atom index.
 // Deterministic for given coordinates.
 __global__ void k_sort_cells(const int* start, int nRanks, int* orig, const double* __restrict__ R,
@@ -251,7 +251,8 @@ __global__ void k_sort_cells(const int* start, int nRanks, int* orig, const doub
 }
 
 // per slot: image cell, type, slot of the atom, and the FP32 position and charge
-// (k_pack_mixed's values, also kept per atom as the build-time reference)
+// (u = M R/L - K, also kept per atom as the build-time reference pos0); per atom
+// the build-time coordinates R0 of the skin check
 __global__ void k_fill_slots(const int* orig, int N, const int4* atomK, const int* type, int4* K, uint8_t* type8,
                              int* slotOf, const double* __restrict__ R, const double* __restrict__ charge,
                              double scale, float4* pos4, float4* pos0, double* __restrict__ R0) {
@@ -307,11 +308,10 @@ __global__ void k_tile_info(const int* start, TileGeom g, int* info, int* maxOut
 // per-step packing
 // ---------------------------------------------------------------------------------
 
-// cell-local position of each slot in units of the cell edge: u = M R/L - K,
-// and the charge.  At a list build (pos0 != NULL) the same values are also kept
-// per atom as the reference for k_pack_delta and the fused step.
+// cell-local position of each slot in units of the cell edge, u = M R/L - K, and
+// the charge, from the coordinates (after a change of the box since the build)
 __global__ void k_pack_mixed(const double* __restrict__ R, const double* __restrict__ charge, const int* orig,
-                             const int4* K, int N, double scale, float4* pos4, float4* pos0) {
+                             const int4* K, int N, double scale, float4* pos4) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= N) return;
   int a = orig[s];
@@ -320,9 +320,7 @@ __global__ void k_pack_mixed(const double* __restrict__ R, const double* __restr
   float uy = (float)(R[3 * a + 1] * scale - (double)k.y);
   float uz = (float)(R[3 * a + 2] * scale - (double)k.z);
   double q = charge[a];
-  const float4 v = make_float4(ux, uy, uz, fabs(q) > 2.220446049250313e-16 ? (float)q : 0.0f);
-  pos4[s] = v;
-  if (pos0) pos0[a] = v;
+  pos4[s] = make_float4(ux, uy, uz, fabs(q) > 2.220446049250313e-16 ? (float)q : 0.0f);
 }
 
 // Between builds, with the box of the last build: u = u0 + (R - R0) M/L, the
@@ -361,8 +359,7 @@ void device_pack(System& s) {
   } else if (*s.Lbox == s.builtL) {
     k_pack_delta<<<bl, th, 0, s.stream>>>(s.dR, s.dR0, g.dOrig, g.dPos0, N, (float)((double)g.M / *s.Lbox), g.dPos4);
   } else {   // the box changed since the build: from the coordinates
-    k_pack_mixed<<<bl, th, 0, s.stream>>>(s.dR, s.dCharge, g.dOrig, g.dK, N, (double)g.M / *s.Lbox, g.dPos4,
-                                          (float4*)nullptr);
+    k_pack_mixed<<<bl, th, 0, s.stream>>>(s.dR, s.dCharge, g.dOrig, g.dK, N, (double)g.M / *s.Lbox, g.dPos4);
   }
   CK(cudaGetLastError());
   prof_end(s, PK_PACK);
