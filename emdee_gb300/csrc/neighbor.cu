@@ -486,51 +486,56 @@ __global__ void BUILD_BOUNDS k_build(BuildArgs A) {
     uint16_t* myList = A.nb + ((size_t)t * capC * A.tileStride + li) * 8;
     int n = 0, nIn = 0;
     for (int pass = 0; pass <= (layered ? 1 : 0) && !none; pass++) {
-      // the 5 cells of a stencil row (dx = -2..2) are consecutive in the halo
-      for (int row = 0; row < 25; row++) {
-        const int hy = hcy + row % 5 - 2, hz = hcz + row / 5 - 2;
-        const int h0 = (hcx - 2) + HW * (hy + HW * hz);
-        int q = off[h0];
-        const int q1 = off[h0 + 5];
-        float xhi = 3.0e38f;
-        if (!MINIMG) {
-          // Atoms of a row are sorted along x.  With rho the distance from atom i
-          // to the row's y-z cross-section, only |x_j - x_i| < sqrt(hi2 - rho^2)
-          // can be inside; a 1e-3 cell margin covers the FP32 rounding of the frame.
-          const float y0 = (float)(hy - g.C), z0 = (float)(hz - g.C);
-          const float dy = fmaxf(fmaxf(y0 - pi.y, pi.y - (y0 + 1.0f)) - 1e-3f, 0.0f);
-          const float dz = fmaxf(fmaxf(z0 - pi.z, pi.z - (z0 + 1.0f)) - 1e-3f, 0.0f);
-          const float rem = A.hi2 - (dy * dy + dz * dz);
-          if (rem <= 0.0f) continue;
-          const float w = sqrtf(rem) + 1e-3f;
-          const float xlo = pi.x - w;
-          xhi = pi.x + w;
-          while (q < q1 && hpos[q].x <= xlo) q++;
-        }
-        for (; q < q1; q++) {
-          const float4 pj = hpos[q];
-          if (!MINIMG && pj.x >= xhi) break;
-          float ex = pi.x - pj.x, ey = pi.y - pj.y, ez = pi.z - pj.z;
-          if (MINIMG) {
-            ex -= A.Mf * rintf(ex / A.Mf);
-            ey -= A.Mf * rintf(ey / A.Mf);
-            ez -= A.Mf * rintf(ez / A.Mf);
+      // the 5 cells of a stencil row (dx = -2..2) are consecutive in the halo;
+      // rows in the order dz = -2..2 (outer), dy = -2..2 (inner)
+      for (int rz = -2; rz <= 2; rz++) {
+        const int hz = hcz + rz;
+        const float z0 = (float)(hz - g.C);
+        const float dz = fmaxf(fmaxf(z0 - pi.z, pi.z - (z0 + 1.0f)) - 1e-3f, 0.0f), dz2 = dz * dz;
+        for (int ry = -2; ry <= 2; ry++) {
+          const int hy = hcy + ry;
+          const int h0 = (hcx - 2) + HW * (hy + HW * hz);
+          int q = off[h0];
+          const int q1 = off[h0 + 5];
+          float xhi = 3.0e38f;
+          if (!MINIMG) {
+            // Atoms of a row are sorted along x.  With rho the distance from atom i
+            // to the row's y-z cross-section, only |x_j - x_i| < sqrt(hi2 - rho^2)
+            // can be inside; a 1e-3 cell margin covers the FP32 rounding of the frame.
+            const float y0 = (float)(hy - g.C);
+            const float dy = fmaxf(fmaxf(y0 - pi.y, pi.y - (y0 + 1.0f)) - 1e-3f, 0.0f);
+            const float rem = A.hi2 - (dy * dy + dz2);
+            if (rem <= 0.0f) continue;
+            const float w = rem * rsqrtf(rem) + 1e-3f;   // approximate square root: within the margin
+            const float xlo = pi.x - w;
+            xhi = pi.x + w;
+            while (q < q1 && hpos[q].x <= xlo) q++;
           }
-          const float r2 = ex * ex + ey * ey + ez * ez;
-          if (r2 >= A.hi2 || q == myq) continue;
-          if (!(r2 < A.lo2 || exact_inside(A.R, A.L, ai, A.orig[hslot[q]], A.thr))) continue;
-          if (GENERAL && !single && !sinter[ti * A.ntypes + htype[q]]) continue;
-          if (filterByAtom) {
-            const int aj = A.orig[hslot[q]];
-            if (A.hasBodies && A.body[aj] == bi) continue;
-            if (hasEx && excluded(A, ai, aj)) continue;
+          for (; q < q1; q++) {
+            const float4 pj = hpos[q];
+            if (!MINIMG && pj.x >= xhi) break;
+            float ex = pi.x - pj.x, ey = pi.y - pj.y, ez = pi.z - pj.z;
+            if (MINIMG) {
+              ex -= A.Mf * rintf(ex / A.Mf);
+              ey -= A.Mf * rintf(ey / A.Mf);
+              ez -= A.Mf * rintf(ez / A.Mf);
+            }
+            const float r2 = ex * ex + ey * ey + ez * ez;
+            if (r2 >= A.hi2 || q == myq) continue;
+            if (!(r2 < A.lo2 || exact_inside(A.R, A.L, ai, A.orig[hslot[q]], A.thr))) continue;
+            if (GENERAL && !single && !sinter[ti * A.ntypes + htype[q]]) continue;
+            if (filterByAtom) {
+              const int aj = A.orig[hslot[q]];
+              if (A.hasBodies && A.body[aj] == bi) continue;
+              if (hasEx && excluded(A, ai, aj)) continue;
+            }
+            if (layered) {
+              bool inner = r2 < A.loIn2 || (r2 < A.hiIn2 && exact_inside(A.R, A.L, ai, A.orig[hslot[q]], A.thrIn));
+              if (inner == (pass == 1)) continue;
+            }
+            if (n < A.cap) myList[(n >> 3) * chunkStride + (n & 7)] = (uint16_t)q;
+            n++;
           }
-          if (layered) {
-            bool inner = r2 < A.loIn2 || (r2 < A.hiIn2 && exact_inside(A.R, A.L, ai, A.orig[hslot[q]], A.thrIn));
-            if (inner == (pass == 1)) continue;
-          }
-          if (n < A.cap) myList[(n >> 3) * chunkStride + (n & 7)] = (uint16_t)q;
-          n++;
         }
       }
       if (pass == 0) nIn = n;
