@@ -162,7 +162,8 @@ __device__ void rep_build(RepShared& S, const double* Rb, float4* pos, int* cell
     stype[s] = (uint8_t)(D.ntypes > 1 ? D.type[a] - 1 : 0);
   }
   __syncthreads();
-  // full lists: 125 stencil cells, candidate order (z, y, x, slot)
+  // full lists: 125 stencil cells, candidate order (z, y, x, slot).  M >= 5, so
+  // a neighbour coordinate c + s (|s| <= 2) wraps by at most one period.
   for (int i = threadIdx.x; i < N; i += THREADS) {
     const int4 ki = D.K[i];
     const int cx = ki.w % M, cy = (ki.w / M) % M, cz = ki.w / (M * M);
@@ -171,7 +172,11 @@ __device__ void rep_build(RepShared& S, const double* Rb, float4* pos, int* cell
     int n = 0;
     for (int code = 0; code < 125; code++) {
       const int sx = code % 5 - 2, sy = (code / 5) % 5 - 2, sz = code / 25 - 2;
-      const int nc = wrap(cx + sx, M) + M * (wrap(cy + sy, M) + M * wrap(cz + sz, M));
+      int nx = cx + sx, ny = cy + sy, nz = cz + sz;
+      nx += nx < 0 ? M : (nx >= M ? -M : 0);
+      ny += ny < 0 ? M : (ny >= M ? -M : 0);
+      nz += nz < 0 ? M : (nz >= M ? -M : 0);
+      const int nc = nx + M * (ny + M * nz);
       const float4 o = offTab[code];
       for (int j = cellStart[nc]; j < cellStart[nc + 1]; j++) {
         if (j == i) continue;
@@ -239,10 +244,10 @@ __global__ void __launch_bounds__(THREADS) k_replicas(const RepDesc* __restrict_
     // boost(dt/2) and displace(dt), FP64 (src/EmDeeData.f90:823-896)
     for (int a = threadIdx.x; a < N; a += THREADS) {
       const double im = D.unitMass ? 1.0 : D.invMass[a];
-      for (int d = 0; d < 3; d++) {
-        const double p = D.P[3 * a + d] + dt_2 * D.F[3 * a + d];
+      for (int d = 0; d < 3; d++) {   // fused multiply-adds, as the single-system mixed path
+        const double p = fma(dt_2, D.F[3 * a + d], D.P[3 * a + d]);
         D.P[3 * a + d] = p;
-        D.R[3 * a + d] = D.unitMass ? D.R[3 * a + d] + dt * p : D.R[3 * a + d] + dt * p * im;
+        D.R[3 * a + d] = D.unitMass ? fma(dt, p, D.R[3 * a + d]) : fma(dt * p, im, D.R[3 * a + d]);
       }
     }
     __syncthreads();
@@ -280,8 +285,8 @@ __global__ void __launch_bounds__(THREADS) k_replicas(const RepDesc* __restrict_
     for (int s = threadIdx.x; s < N; s += THREADS) {
       const int a = D.orig[s];
       const int4 kk = D.K[s];
-      pos[s] = make_float4((float)(D.R[3 * a] * D.scale - (double)kk.x), (float)(D.R[3 * a + 1] * D.scale - (double)kk.y),
-                           (float)(D.R[3 * a + 2] * D.scale - (double)kk.z), 0.f);
+      pos[s] = make_float4((float)fma(D.R[3 * a], D.scale, -(double)kk.x), (float)fma(D.R[3 * a + 1], D.scale, -(double)kk.y),
+                           (float)fma(D.R[3 * a + 2], D.scale, -(double)kk.z), 0.f);
     }
     __syncthreads();
     // pair forces (full lists, no atomics); energies on compute steps, virial every step
@@ -358,7 +363,7 @@ __global__ void __launch_bounds__(THREADS) k_replicas(const RepDesc* __restrict_
     for (int a = threadIdx.x; a < N; a += THREADS) {
       const double im = D.unitMass ? 1.0 : D.invMass[a];
       for (int d = 0; d < 3; d++) {
-        const double p = D.P[3 * a + d] + dt_2 * D.F[3 * a + d];
+        const double p = fma(dt_2, D.F[3 * a + d], D.P[3 * a + d]);
         D.P[3 * a + d] = p;
         if (compute) ke[d] += im * (p * p);
       }
