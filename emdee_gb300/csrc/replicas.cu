@@ -202,6 +202,68 @@ __device__ void rep_build(RepShared& S, const double* Rb, float4* pos, int* cell
   __syncthreads();
 }
 
+// Pair forces of one replica (full lists, one thread per slot, no atomics).  LJ:
+// single-type lj_cut without modifier, with the Lennard-Jones arithmetic in cell
+// units (E = 4 eps sr6 (sr6 - 1), W = 24 eps sr6 (2 sr6 - 1)); otherwise the
+// general model code.  COMPUTE: energies too (the virial is always summed).
+template <bool LJ, bool COMPUTE>
+__device__ __forceinline__ void rep_pairs(const RepDesc& D, const float4* pos, const float4* offTab,
+                                          const NBParams<float>* ptab, const uint8_t* stype, float& Ep, float& Wp) {
+  const NBParams<float> mdl = D.model.model;
+  const int nt = D.ntypes, N = D.N;
+  const float rc2 = D.rc2, invw2 = D.invw2, invw = D.invw, Mf = D.Mf;
+  const float sigc = mdl.sigsq * invw2, eps48 = 2.0f * mdl.eps24;
+  const bool minimg = D.minimg;
+  const int cap = D.cap;
+  const uint32_t* __restrict__ list = D.list;
+  const int* __restrict__ count = D.count;
+  const int* __restrict__ orig = D.orig;
+  double* __restrict__ F = D.F;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    const float4 pi = pos[i];
+    const int n = min(count[i], cap);
+    const NBParams<float>* row = ptab + (nt > 1 ? stype[i] * nt : 0);
+    float fx = 0.f, fy = 0.f, fz = 0.f;
+    for (int q = 0; q < n; q++) {
+      const uint32_t e = __ldg(&list[(size_t)q * N + i]);
+      const int j = e & 0xFFFFu;
+      const float4 pj = pos[j];
+      const float4 o = offTab[e >> 16];
+      float dx = (pi.x - pj.x) - o.x, dy = (pi.y - pj.y) - o.y, dz = (pi.z - pj.z) - o.z;
+      if (minimg) {
+        dx -= Mf * rintf(dx / Mf);
+        dy -= Mf * rintf(dy / Mf);
+        dz -= Mf * rintf(dz / Mf);
+      }
+      const float r2 = dx * dx + dy * dy + dz * dz;
+      const bool in = r2 < rc2;
+      const float invR2c = Ops<float>::rcp(r2);
+      float E = 0.f, W;
+      if (LJ) {
+        const float sr2 = sigc * invR2c, sr6 = sr2 * sr2 * sr2;
+        W = sr6 * fmaf(eps48, sr6, -mdl.eps24);
+        if (COMPUTE) E = sr6 * fmaf(mdl.eps4, sr6, -mdl.eps4);
+      } else {
+        const float invR2 = invR2c * invw2, invR = sqrtf(invR2);
+        const NBParams<float>& m = nt == 1 ? mdl : row[stype[j]];
+        nb_compute(m, E, W, invR, invR2);
+        modifier_compute(m, E, W, invR, invR2);
+      }
+      W = in ? W : 0.f;
+      if (COMPUTE) Ep += in ? E : 0.f;
+      Wp += W;
+      const float sc = W * invR2c;
+      fx += sc * dx;
+      fy += sc * dy;
+      fz += sc * dz;
+    }
+    const int a = orig[i];
+    F[3 * a] = f2d_exact(fx * invw);
+    F[3 * a + 1] = f2d_exact(fy * invw);
+    F[3 * a + 2] = f2d_exact(fz * invw);
+  }
+}
+
 template <int THREADS>
 __global__ void __launch_bounds__(THREADS) k_replicas(const RepDesc* __restrict__ descs, const int* __restrict__ order,
                                                       int steps, double dt, int nprop, int Nmax, int cellsMax) {
@@ -291,57 +353,12 @@ __global__ void __launch_bounds__(THREADS) k_replicas(const RepDesc* __restrict_
     __syncthreads();
     // pair forces (full lists, no atomics); energies on compute steps, virial every step
     float Ep = 0.f, Wp = 0.f;
-    {
-      const NBParams<float> mdl = D.model.model;
-      const int nt = D.ntypes;
-      const float rc2 = D.rc2, invw2 = D.invw2, invw = D.invw, Mf = D.Mf;
-      const bool minimg = D.minimg;
-      const int cap = D.cap;
-      const uint32_t* __restrict__ list = D.list;
-      const int* __restrict__ count = D.count;
-      const int* __restrict__ orig = D.orig;
-      double* __restrict__ F = D.F;
-      for (int i = threadIdx.x; i < N; i += THREADS) {
-        const float4 pi = pos[i];
-        const int n = min(count[i], cap);
-        const NBParams<float>* row = ptab + (nt > 1 ? stype[i] * nt : 0);
-        float fx = 0.f, fy = 0.f, fz = 0.f;
-        for (int q = 0; q < n; q++) {
-          const uint32_t e = __ldg(&list[(size_t)q * N + i]);
-          const int j = e & 0xFFFFu;
-          const float4 pj = pos[j];
-          const float4 o = offTab[e >> 16];
-          float dx = (pi.x - pj.x) - o.x, dy = (pi.y - pj.y) - o.y, dz = (pi.z - pj.z) - o.z;
-          if (minimg) {
-            dx -= Mf * rintf(dx / Mf);
-            dy -= Mf * rintf(dy / Mf);
-            dz -= Mf * rintf(dz / Mf);
-          }
-          const float r2 = dx * dx + dy * dy + dz * dz;
-          const bool in = r2 < rc2;
-          const float invR2c = Ops<float>::rcp(r2), invR2 = invR2c * invw2, invR = sqrtf(invR2);
-          float E, W;
-          if (nt == 1) {
-            nb_compute(mdl, E, W, invR, invR2);
-            modifier_compute(mdl, E, W, invR, invR2);
-          } else {
-            const NBParams<float>& m = row[stype[j]];
-            nb_compute(m, E, W, invR, invR2);
-            modifier_compute(m, E, W, invR, invR2);
-          }
-          W = in ? W : 0.f;
-          Ep += in ? E : 0.f;
-          Wp += W;
-          const float sc = W * invR2c;
-          fx += sc * dx;
-          fy += sc * dy;
-          fz += sc * dz;
-        }
-        const int a = orig[i];
-        F[3 * a] = f2d_exact(fx * invw);
-        F[3 * a + 1] = f2d_exact(fy * invw);
-        F[3 * a + 2] = f2d_exact(fz * invw);
-      }
+    const bool lj = D.ntypes == 1 && D.model.model.kind == MK_LJ_CUT && D.model.model.modifier == NONE;
+    if (lj) {
+      if (compute) rep_pairs<true, true>(D, pos, offTab, ptab, stype, Ep, Wp);
+      else rep_pairs<true, false>(D, pos, offTab, ptab, stype, Ep, Wp);
+    } else {
+      rep_pairs<false, true>(D, pos, offTab, ptab, stype, Ep, Wp);
     }
     {
       float hi[2] = {0.5f * Ep, 0.5f * Wp}, lo[2] = {0.f, 0.f};
