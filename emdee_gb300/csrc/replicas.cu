@@ -45,7 +45,7 @@ struct RepDesc {
   int* orig;        // slot -> atom
   int4* K;          // per slot: build-time unwrapped cell (x, y, z), cell rank (w)
   int4* atomK;      // per atom scratch of the same
-  uint32_t* list;   // entry n of slot i at list[n * N + i]
+  uint32_t* list;   // entries 4c..4c+3 of slot i: the 16 bytes at list[(c * N + i) * 4]
   int* count;       // per slot
   double* out;      // [0] Epair [1] Wpair [2..4] 2KE per dim [5] builds [6] overflow [7] steps done
   int computeLast;  // unused by the kernel (host bookkeeping)
@@ -190,7 +190,7 @@ __device__ void rep_build(RepShared& S, const double* Rb, float4* pos, int* cell
         const float r2 = dx * dx + dy * dy + dz * dz;
         if (r2 >= D.hi2) continue;
         if (!(r2 < D.lo2) && !rep_exact_inside(Rb, D.L, ai, D.orig[j], D.thr)) continue;
-        if (n < D.cap) D.list[(size_t)n * N + i] = (uint32_t)j | ((uint32_t)code << 16);
+        if (n < D.cap) D.list[((size_t)(n >> 2) * N + i) * 4 + (n & 3)] = (uint32_t)j | ((uint32_t)code << 16);
         n++;
       }
     }
@@ -215,7 +215,7 @@ __device__ __forceinline__ void rep_pairs(const RepDesc& D, const float4* pos, c
   const float sigc = mdl.sigsq * invw2, eps48 = 2.0f * mdl.eps24;
   const bool minimg = D.minimg;
   const int cap = D.cap;
-  const uint32_t* __restrict__ list = D.list;
+  const uint4* __restrict__ list = reinterpret_cast<const uint4*>(D.list);
   const int* __restrict__ count = D.count;
   const int* __restrict__ orig = D.orig;
   double* __restrict__ F = D.F;
@@ -224,38 +224,48 @@ __device__ __forceinline__ void rep_pairs(const RepDesc& D, const float4* pos, c
     const int n = min(count[i], cap);
     const NBParams<float>* row = ptab + (nt > 1 ? stype[i] * nt : 0);
     float fx = 0.f, fy = 0.f, fz = 0.f;
-    for (int q = 0; q < n; q++) {
-      const uint32_t e = __ldg(&list[(size_t)q * N + i]);
-      const int j = e & 0xFFFFu;
-      const float4 pj = pos[j];
-      const float4 o = offTab[e >> 16];
-      float dx = (pi.x - pj.x) - o.x, dy = (pi.y - pj.y) - o.y, dz = (pi.z - pj.z) - o.z;
-      if (minimg) {
-        dx -= Mf * rintf(dx / Mf);
-        dy -= Mf * rintf(dy / Mf);
-        dz -= Mf * rintf(dz / Mf);
+    const int nch = (n + 3) >> 2;
+    // 4 entries per 16-byte load, the next chunk requested before this one is used
+    uint4 cur = nch > 0 ? __ldg(&list[i]) : make_uint4(0u, 0u, 0u, 0u);
+    for (int c = 0; c < nch; c++) {
+      const uint4 nxt = c + 1 < nch ? __ldg(&list[(size_t)(c + 1) * N + i]) : cur;
+      const uint32_t w[4] = {cur.x, cur.y, cur.z, cur.w};
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        if (4 * c + u >= n) break;
+        const uint32_t e = w[u];
+        const int j = e & 0xFFFFu;
+        const float4 pj = pos[j];
+        const float4 o = offTab[e >> 16];
+        float dx = (pi.x - pj.x) - o.x, dy = (pi.y - pj.y) - o.y, dz = (pi.z - pj.z) - o.z;
+        if (minimg) {
+          dx -= Mf * rintf(dx / Mf);
+          dy -= Mf * rintf(dy / Mf);
+          dz -= Mf * rintf(dz / Mf);
+        }
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        const bool in = r2 < rc2;
+        const float invR2c = Ops<float>::rcp(r2);
+        float E = 0.f, W;
+        if (LJ) {
+          const float sr2 = sigc * invR2c, sr6 = sr2 * sr2 * sr2;
+          W = sr6 * fmaf(eps48, sr6, -mdl.eps24);
+          if (COMPUTE) E = sr6 * fmaf(mdl.eps4, sr6, -mdl.eps4);
+        } else {
+          const float invR2 = invR2c * invw2, invR = sqrtf(invR2);
+          const NBParams<float>& m = nt == 1 ? mdl : row[stype[j]];
+          nb_compute(m, E, W, invR, invR2);
+          modifier_compute(m, E, W, invR, invR2);
+        }
+        W = in ? W : 0.f;
+        if (COMPUTE) Ep += in ? E : 0.f;
+        Wp += W;
+        const float sc = W * invR2c;
+        fx += sc * dx;
+        fy += sc * dy;
+        fz += sc * dz;
       }
-      const float r2 = dx * dx + dy * dy + dz * dz;
-      const bool in = r2 < rc2;
-      const float invR2c = Ops<float>::rcp(r2);
-      float E = 0.f, W;
-      if (LJ) {
-        const float sr2 = sigc * invR2c, sr6 = sr2 * sr2 * sr2;
-        W = sr6 * fmaf(eps48, sr6, -mdl.eps24);
-        if (COMPUTE) E = sr6 * fmaf(mdl.eps4, sr6, -mdl.eps4);
-      } else {
-        const float invR2 = invR2c * invw2, invR = sqrtf(invR2);
-        const NBParams<float>& m = nt == 1 ? mdl : row[stype[j]];
-        nb_compute(m, E, W, invR, invR2);
-        modifier_compute(m, E, W, invR, invR2);
-      }
-      W = in ? W : 0.f;
-      if (COMPUTE) Ep += in ? E : 0.f;
-      Wp += W;
-      const float sc = W * invR2c;
-      fx += sc * dx;
-      fy += sc * dy;
-      fz += sc * dz;
+      cur = nxt;
     }
     const int a = orig[i];
     F[3 * a] = f2d_exact(fx * invw);
@@ -564,7 +574,7 @@ void* EmDee_replicas_create(int n, tEmDee** systems) {
     d.type = s.dType;
     // list capacity: twice the ideal-gas count within rc+skin, at least 64
     const double expect = 4.0 / 3.0 * 3.14159265358979 * std::pow(s.xRc, 3) * s.natoms / (L * L * L);
-    d.cap = std::max(64, ((int)(2.0 * expect) + 7) / 8 * 8);
+    d.cap = std::max(64, ((int)(2.0 * expect) + 7) / 8 * 8);   // a multiple of the 4-entry chunk
     CK(cudaMalloc(&d.orig, sizeof(int) * d.N));
     CK(cudaMalloc(&d.K, sizeof(int4) * d.N));
     CK(cudaMalloc(&d.atomK, sizeof(int4) * d.N));
