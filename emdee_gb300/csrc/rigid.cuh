@@ -271,24 +271,34 @@ RB_HDN inline void rb_rotate_exact(BodyState& b, double dt, const double* d, dou
   double sn, cn, dn, deltaF;
   rb_jacobi(u, m, sn, cn, dn);
   double alpha = b.MoI[0] * a[0] / L;
+  // The two cases of src/ArBee.f90 (l1 < l3 or not) differ only in scalar set-up;
+  // the elliptic integrals are evaluated by one common code path so that the
+  // bodies of a warp do not run them twice (once per case) on the device.
+  const double eta = alpha * alpha / (1.0 - alpha * alpha);
+  double nTheta, C, y1, y0, extra;
   if (l1 < l3) {
     b.omega[0] = a[0] * cn; b.omega[1] = a[1] * sn; b.omega[2] = a[2] * dn;
     double d0 = w0[2] / a[2];
-    double eta = alpha * alpha / (1.0 - alpha * alpha), C = sqrt(m + eta);
-    double r = u - u0 + rb_sign(1.0, cn) * rb_Theta(sn, eta, m) - rb_sign(1.0, c0) * rb_Theta(s0, eta, m) +
-               (alpha / C) * (atan(C * sn / dn) - atan(C * s0 / d0));
-    if (jump != 0) r += jump * 2.0 * rb_Theta(1.0, eta, m);
-    deltaF = (eta + 1.0) * r;
+    nTheta = eta;
+    C = sqrt(m + eta);
+    y1 = C * sn / dn;
+    y0 = C * s0 / d0;
+    extra = 0.0;
   } else {
     b.omega[0] = a[0] * dn; b.omega[1] = a[1] * sn; b.omega[2] = a[2] * cn;
-    double eta = alpha * alpha;
-    eta = eta / (1.0 - eta);
-    double k2eta = m * eta, C = sqrt(1.0 + k2eta);
-    double r = u - u0 + rb_sign(1.0, cn) * rb_Theta(sn, k2eta, m) - rb_sign(1.0, c0) * rb_Theta(s0, k2eta, m) +
-               (alpha / C) * (atan(C * sn / cn) - atan(C * s0 / c0));
-    if (jump != 0) r += jump * (2.0 * rb_Theta(1.0, k2eta, m) + (alpha / C) * PI);
-    deltaF = (eta + 1.0) * r;
+    nTheta = m * eta;
+    C = sqrt(1.0 + nTheta);
+    y1 = C * sn / cn;
+    y0 = C * s0 / c0;
+    extra = (alpha / C) * PI;
   }
+  double r = u - u0 + rb_sign(1.0, cn) * rb_Theta(sn, nTheta, m) - rb_sign(1.0, c0) * rb_Theta(s0, nTheta, m) +
+             (alpha / C) * (atan(y1) - atan(y0));
+  if (jump != 0) {
+    const double T1 = rb_Theta(1.0, nTheta, m);
+    r += l1 < l3 ? jump * 2.0 * T1 : jump * (2.0 * T1 + extra);
+  }
+  deltaF = (eta + 1.0) * r;
   double phi = (Lsq * (u - u0) + r3 * deltaF) / (2.0 * L * b.MoI[0] * wp);
   double z0[4] = {Iw[2], Iw[1], L - Iw[0], 0.0};
   for (int k = 0; k < 3; k++) Iw[k] = b.MoI[k] * b.omega[k];
