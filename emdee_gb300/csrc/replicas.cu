@@ -40,6 +40,7 @@ struct RepDesc {
   float lo2, hi2, rc2, invw2, invw, Mf;
   PairEntry<float> model;          // type pair (1, 1)
   int ntypes;
+  int ljAll;                       // every type pair is lj_cut without modifier
   const PairEntry<float>* table;   // the system's layer-1 pair table, [jtype][itype]
   const int* type;                 // atom types (1-based, API order)
   int* orig;        // slot -> atom
@@ -203,7 +204,7 @@ __device__ void rep_build(RepShared& S, const double* Rb, float4* pos, int* cell
 }
 
 // Pair forces of one replica (full lists, one thread per slot, no atomics).  LJ:
-// single-type lj_cut without modifier, with the Lennard-Jones arithmetic in cell
+// every type pair lj_cut without modifier, with the Lennard-Jones arithmetic in cell
 // units (E = 4 eps sr6 (sr6 - 1), W = 24 eps sr6 (2 sr6 - 1)); otherwise the
 // general model code.  COMPUTE: energies too (the virial is always summed).
 template <bool LJ, bool COMPUTE>
@@ -248,9 +249,17 @@ __device__ __forceinline__ void rep_pairs(const RepDesc& D, const float4* pos, c
         const float invR2c = Ops<float>::rcp(r2);
         float E = 0.f, W;
         if (LJ) {
-          const float sr2 = sigc * invR2c, sr6 = sr2 * sr2 * sr2;
-          W = sr6 * fmaf(eps48, sr6, -mdl.eps24);
-          if (COMPUTE) E = sr6 * fmaf(mdl.eps4, sr6, -mdl.eps4);
+          float sg = sigc, e48 = eps48, e24 = mdl.eps24, e4 = mdl.eps4;
+          if (nt > 1) {
+            const NBParams<float>& m = row[stype[j]];
+            sg = m.sigsq * invw2;
+            e24 = m.eps24;
+            e48 = 2.0f * e24;
+            e4 = m.eps4;
+          }
+          const float sr2 = sg * invR2c, sr6 = sr2 * sr2 * sr2;
+          W = sr6 * fmaf(e48, sr6, -e24);
+          if (COMPUTE) E = sr6 * fmaf(e4, sr6, -e4);
         } else {
           const float invR2 = invR2c * invw2, invR = sqrtf(invR2);
           const NBParams<float>& m = nt == 1 ? mdl : row[stype[j]];
@@ -363,7 +372,7 @@ __global__ void __launch_bounds__(THREADS) k_replicas(const RepDesc* __restrict_
     __syncthreads();
     // pair forces (full lists, no atomics); energies on compute steps, virial every step
     float Ep = 0.f, Wp = 0.f;
-    const bool lj = D.ntypes == 1 && D.model.model.kind == MK_LJ_CUT && D.model.model.modifier == NONE;
+    const bool lj = D.ljAll != 0;
     if (lj) {
       if (compute) rep_pairs<true, true>(D, pos, offTab, ptab, stype, Ep, Wp);
       else rep_pairs<true, false>(D, pos, offTab, ptab, stype, Ep, Wp);
@@ -571,6 +580,12 @@ void* EmDee_replicas_create(int n, tEmDee** systems) {
     CK(cudaMemcpy(&d.model, s.models.d32, sizeof(PairEntry<float>), cudaMemcpyDeviceToHost));
     d.ntypes = s.ntypes;
     d.table = s.models.d32;
+    d.ljAll = 1;
+    for (int ti = 0; ti < s.ntypes; ti++)
+      for (int tj = 0; tj < s.ntypes; tj++) {
+        const NBParams<double>& m = s.P(ti, tj, 0).model.p;
+        if (!(m.kind == MK_LJ_CUT && m.modifier == NONE)) d.ljAll = 0;
+      }
     d.type = s.dType;
     // list capacity: twice the ideal-gas count within rc+skin, at least 64
     const double expect = 4.0 / 3.0 * 3.14159265358979 * std::pow(s.xRc, 3) * s.natoms / (L * L * L);
