@@ -399,6 +399,7 @@ struct BuildArgs {
   int* nbInner;
   uint16_t* selfIdx;
   int cap, tileStride;
+  int tpa, tpaShift;   // threads per atom of the split build (a power of 2) and its log2
   int* maxCount;
 };
 
@@ -423,7 +424,8 @@ __device__ __forceinline__ bool excluded(const BuildArgs& A, int a, int b) {
   return false;
 }
 
-static const int BUILD_THREADS = 256;   // upper bound; launches use one thread per tile atom
+static const int BUILD_THREADS = 256;         // upper bound; launches use one thread per tile atom
+static const int BUILD_THREADS_SPLIT = 1024;  // split build: several threads per tile atom
 
 // List layout: for tile t, chunk c (8 entries) and tile-local atom li, the
 // entries 8c..8c+7 of atom li are 16 contiguous bytes at
@@ -437,11 +439,11 @@ __device__ __forceinline__ size_t nb_index(int t, int capC, int tileStride, int 
 // GENERAL: several atom types, bodies, exclusions or layered lists; MINIMG: M = 5.
 // BUILD_MIN_BLOCKS (compile-time): resident blocks per SM the register budget must allow
 #ifdef BUILD_MIN_BLOCKS
-#define BUILD_BOUNDS __launch_bounds__(BUILD_THREADS, BUILD_MIN_BLOCKS)
+#define BUILD_BOUNDS __launch_bounds__(SPLIT ? BUILD_THREADS_SPLIT : BUILD_THREADS, BUILD_MIN_BLOCKS)
 #else
-#define BUILD_BOUNDS __launch_bounds__(BUILD_THREADS)
+#define BUILD_BOUNDS __launch_bounds__(SPLIT ? BUILD_THREADS_SPLIT : BUILD_THREADS)
 #endif
-template <bool GENERAL, bool MINIMG>
+template <bool GENERAL, bool MINIMG, bool SPLIT>
 __global__ void BUILD_BOUNDS k_build(BuildArgs A) {
   extern __shared__ __align__(16) unsigned char sraw[];
   __shared__ int ws[33];
@@ -473,77 +475,128 @@ __global__ void BUILD_BOUNDS k_build(BuildArgs A) {
   const bool layered = GENERAL && A.layered;
   const int tb = A.start[t * cells], te = A.start[(t + 1) * cells];
   const int HW = g.HW, capC = A.cap >> 3, chunkStride = A.tileStride * 8;
-  for (int li = threadIdx.x; li < te - tb; li += blockDim.x) {
+  // SPLIT: tpa threads share an atom, each scanning the stencil rows r = sub,
+  // sub + tpa, ...; a first sweep counts the accepted entries (inner and outer),
+  // the group's prefix sums give each thread its output positions, and a second
+  // sweep writes them.  The list order is then (thread, row, halo index) -- a
+  // deterministic function of the coordinates, like the single-thread order.
+  const int tpa = SPLIT ? A.tpa : 1, sub = SPLIT ? (int)(threadIdx.x & (tpa - 1)) : 0;
+  const int tshift = SPLIT ? A.tpaShift : 0;
+  const unsigned gmask = (0xFFFFFFFFu >> (32 - tpa)) << ((threadIdx.x & 31) & ~(tpa - 1));
+  for (int li = threadIdx.x >> tshift; li < te - tb; li += blockDim.x >> tshift) {
     const int si = tb + li;
     const int rank = A.K[si].w, lr = rank - t * cells;
     const int hcx = lr % g.TB + 2, hcy = (lr / g.TB) % g.TB + 2, hcz = lr / (g.TB * g.TB) + 2;
     const int myq = off[hcx + HW * (hcy + HW * hcz)] + (si - A.start[rank]);
-    A.selfIdx[si] = (uint16_t)myq;
+    if (sub == 0) A.selfIdx[si] = (uint16_t)myq;
     const float4 pi = hpos[myq];
     const int ai = A.orig[si], ti = single ? 0 : A.type8[si];
     const int bi = filterByAtom && A.hasBodies ? A.body[ai] : -1;
     const bool hasEx = filterByAtom && A.hasEx && A.exCount[ai] > 0;
     uint16_t* myList = A.nb + ((size_t)t * capC * A.tileStride + li) * 8;
+    // accepted candidates of stencil row (rz, ry) -> f(q, inner); the 5 cells of a
+    // row (dx = -2..2) are consecutive in the halo
+    auto zdist2 = [&](int rz) {   // squared distance from atom i to the z slab of offset rz
+      const float z0 = (float)(hcz + rz - g.C);
+      const float dz = fmaxf(fmaxf(z0 - pi.z, pi.z - (z0 + 1.0f)) - 1e-3f, 0.0f);
+      return dz * dz;
+    };
+    auto row = [&](int rz, int ry, float dz2, auto&& f) {
+      const int hz = hcz + rz, hy = hcy + ry;
+      const int h0 = (hcx - 2) + HW * (hy + HW * hz);
+      int q = off[h0];
+      const int q1 = off[h0 + 5];
+      float xhi = 3.0e38f;
+      if (!MINIMG) {
+        // Atoms of a row are sorted along x.  With rho the distance from atom i
+        // to the row's y-z cross-section, only |x_j - x_i| < sqrt(hi2 - rho^2)
+        // can be inside; a 1e-3 cell margin covers the FP32 rounding of the frame.
+        const float y0 = (float)(hy - g.C);
+        const float dy = fmaxf(fmaxf(y0 - pi.y, pi.y - (y0 + 1.0f)) - 1e-3f, 0.0f);
+        const float rem = A.hi2 - (dy * dy + dz2);
+        if (rem <= 0.0f) return;
+        const float w = rem * rsqrtf(rem) + 1e-3f;   // approximate square root: within the margin
+        const float xlo = pi.x - w;
+        xhi = pi.x + w;
+        while (q < q1 && hpos[q].x <= xlo) q++;
+      }
+      for (; q < q1; q++) {
+        const float4 pj = hpos[q];
+        if (!MINIMG && pj.x >= xhi) break;
+        float ex = pi.x - pj.x, ey = pi.y - pj.y, ez = pi.z - pj.z;
+        if (MINIMG) {
+          ex -= A.Mf * rintf(ex / A.Mf);
+          ey -= A.Mf * rintf(ey / A.Mf);
+          ez -= A.Mf * rintf(ez / A.Mf);
+        }
+        const float r2 = ex * ex + ey * ey + ez * ez;
+        if (r2 >= A.hi2 || q == myq) continue;
+        if (!(r2 < A.lo2 || exact_inside(A.R, A.L, ai, A.orig[hslot[q]], A.thr))) continue;
+        if (GENERAL && !single && !sinter[ti * A.ntypes + htype[q]]) continue;
+        if (filterByAtom) {
+          const int aj = A.orig[hslot[q]];
+          if (A.hasBodies && A.body[aj] == bi) continue;
+          if (hasEx && excluded(A, ai, aj)) continue;
+        }
+        bool inner = true;
+        if (layered)
+          inner = r2 < A.loIn2 || (r2 < A.hiIn2 && exact_inside(A.R, A.L, ai, A.orig[hslot[q]], A.thrIn));
+        f(q, inner);
+      }
+    };
+    auto put = [&](int k, int q) {
+      if (k < A.cap) myList[(k >> 3) * chunkStride + (k & 7)] = (uint16_t)q;
+    };
     int n = 0, nIn = 0;
-    for (int pass = 0; pass <= (layered ? 1 : 0) && !none; pass++) {
-      // the 5 cells of a stencil row (dx = -2..2) are consecutive in the halo;
-      // rows in the order dz = -2..2 (outer), dy = -2..2 (inner)
-      for (int rz = -2; rz <= 2; rz++) {
-        const int hz = hcz + rz;
-        const float z0 = (float)(hz - g.C);
-        const float dz = fmaxf(fmaxf(z0 - pi.z, pi.z - (z0 + 1.0f)) - 1e-3f, 0.0f), dz2 = dz * dz;
-        for (int ry = -2; ry <= 2; ry++) {
-          const int hy = hcy + ry;
-          const int h0 = (hcx - 2) + HW * (hy + HW * hz);
-          int q = off[h0];
-          const int q1 = off[h0 + 5];
-          float xhi = 3.0e38f;
-          if (!MINIMG) {
-            // Atoms of a row are sorted along x.  With rho the distance from atom i
-            // to the row's y-z cross-section, only |x_j - x_i| < sqrt(hi2 - rho^2)
-            // can be inside; a 1e-3 cell margin covers the FP32 rounding of the frame.
-            const float y0 = (float)(hy - g.C);
-            const float dy = fmaxf(fmaxf(y0 - pi.y, pi.y - (y0 + 1.0f)) - 1e-3f, 0.0f);
-            const float rem = A.hi2 - (dy * dy + dz2);
-            if (rem <= 0.0f) continue;
-            const float w = rem * rsqrtf(rem) + 1e-3f;   // approximate square root: within the margin
-            const float xlo = pi.x - w;
-            xhi = pi.x + w;
-            while (q < q1 && hpos[q].x <= xlo) q++;
-          }
-          for (; q < q1; q++) {
-            const float4 pj = hpos[q];
-            if (!MINIMG && pj.x >= xhi) break;
-            float ex = pi.x - pj.x, ey = pi.y - pj.y, ez = pi.z - pj.z;
-            if (MINIMG) {
-              ex -= A.Mf * rintf(ex / A.Mf);
-              ey -= A.Mf * rintf(ey / A.Mf);
-              ez -= A.Mf * rintf(ez / A.Mf);
-            }
-            const float r2 = ex * ex + ey * ey + ez * ez;
-            if (r2 >= A.hi2 || q == myq) continue;
-            if (!(r2 < A.lo2 || exact_inside(A.R, A.L, ai, A.orig[hslot[q]], A.thr))) continue;
-            if (GENERAL && !single && !sinter[ti * A.ntypes + htype[q]]) continue;
-            if (filterByAtom) {
-              const int aj = A.orig[hslot[q]];
-              if (A.hasBodies && A.body[aj] == bi) continue;
-              if (hasEx && excluded(A, ai, aj)) continue;
-            }
-            if (layered) {
-              bool inner = r2 < A.loIn2 || (r2 < A.hiIn2 && exact_inside(A.R, A.L, ai, A.orig[hslot[q]], A.thrIn));
-              if (inner == (pass == 1)) continue;
-            }
-            if (n < A.cap) myList[(n >> 3) * chunkStride + (n & 7)] = (uint16_t)q;
-            n++;
-          }
+    if (!SPLIT) {
+      // rows in the order dz = -2..2 (outer), dy = -2..2 (inner); layered lists
+      // take the inner entries in a first sweep and the outer ones in a second
+      for (int pass = 0; pass <= (layered ? 1 : 0) && !none; pass++) {
+        for (int rz = -2; rz <= 2; rz++) {
+          const float dz2 = MINIMG ? 0.0f : zdist2(rz);
+          for (int ry = -2; ry <= 2; ry++)
+            row(rz, ry, dz2, [&](int q, bool inner) {
+              if (layered && inner == (pass == 1)) return;
+              put(n++, q);
+            });
+        }
+        if (pass == 0) nIn = n;
+      }
+    } else {
+      int cIn = 0, cOut = 0;
+      if (!none)
+        for (int r = sub; r < 25; r += tpa)
+          row(r / 5 - 2, r % 5 - 2, MINIMG ? 0.0f : zdist2(r / 5 - 2), [&](int, bool inner) {
+            if (inner) cIn++;
+            else cOut++;
+          });
+      // exclusive prefix sums over the group's threads, in sub order
+      int pIn = cIn, pOut = cOut;
+      for (int o = 1; o < tpa; o <<= 1) {
+        const int yIn = __shfl_up_sync(gmask, pIn, o), yOut = __shfl_up_sync(gmask, pOut, o);
+        if (sub >= o) {
+          pIn += yIn;
+          pOut += yOut;
         }
       }
-      if (pass == 0) nIn = n;
+      const int totIn = __shfl_sync(gmask, pIn, tpa - 1, tpa), totOut = __shfl_sync(gmask, pOut, tpa - 1, tpa);
+      int kIn = pIn - cIn, kOut = totIn + pOut - cOut;
+      if (!none)
+        for (int r = sub; r < 25; r += tpa)
+          row(r / 5 - 2, r % 5 - 2, MINIMG ? 0.0f : zdist2(r / 5 - 2), [&](int q, bool inner) {
+            if (inner) put(kIn++, q);
+            else put(kOut++, q);
+          });
+      n = totIn + totOut;
+      nIn = totIn;
+      __syncwarp(gmask);
     }
-    for (int k = n; k < A.cap && (k & 7); k++) myList[(k >> 3) * chunkStride + (k & 7)] = (uint16_t)A.haloCap;
-    A.nbCount[si] = n;
-    A.nbInner[si] = nIn;
-    atomicMax(A.maxCount, n);
+    if (sub == 0) {
+      for (int k = n; k < A.cap && (k & 7); k++) myList[(k >> 3) * chunkStride + (k & 7)] = (uint16_t)A.haloCap;
+      A.nbCount[si] = n;
+      A.nbInner[si] = nIn;
+      atomicMax(A.maxCount, n);
+    }
   }
 }
 
@@ -715,8 +768,27 @@ static bool build_lists(System& s, bool reuse) {
   A.maxCount = g.dTileInfo + 2 * g.nTiles + 2;
   size_t smem = build_smem(g, s.ntypes);
   const bool general = s.ntypes > 1 || A.hasBodies || A.hasEx || A.layered;
-  auto kb = general ? (A.minimg ? k_build<true, true> : k_build<true, false>)
-                    : (A.minimg ? k_build<false, true> : k_build<false, false>);
+  // Threads per atom: a system too small to fill the GPU with one thread per atom and
+  // with long lists (more than 48 entries per thread) splits the stencil rows of each
+  // atom over 2, 4 or 8 threads (blocks of up to 1024 threads).
+  {
+    const double expected = N / (L * L * L) * 4.18879020478639 * s.xRcSq * s.xRc;
+    int tpa = 1, shift = 0;
+    while (tpa < 8 && g.tileStride * tpa * 2 <= BUILD_THREADS_SPLIT && (double)N * tpa * 2 <= 152.0 * 2048 &&
+           expected / (tpa * 2) >= 48) {
+      tpa *= 2;
+      shift++;
+    }
+    A.tpa = tpa;
+    A.tpaShift = shift;
+  }
+  const bool split = A.tpa > 1;
+  auto kb = split ? (general ? (A.minimg ? k_build<true, true, true> : k_build<true, false, true>)
+                             : (A.minimg ? k_build<false, true, true> : k_build<false, false, true>))
+                  : (general ? (A.minimg ? k_build<true, true, false> : k_build<true, false, false>)
+                             : (A.minimg ? k_build<false, true, false> : k_build<false, false, false>));
+  const int buildThreads = split ? std::min(BUILD_THREADS_SPLIT, g.tileStride * A.tpa)
+                                 : std::min(BUILD_THREADS, std::max(32, g.tileStride));
   CK(cudaFuncSetAttribute(kb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
 #ifdef EMDEE_MAX_CARVEOUT
   CK(cudaFuncSetAttribute(kb, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared));
@@ -727,7 +799,7 @@ static bool build_lists(System& s, bool reuse) {
     A.nb = g.dNb;
     A.cap = g.cap;
     CK(cudaMemsetAsync(A.maxCount, 0, sizeof(int), s.stream));
-    kb<<<g.nTiles, std::min(BUILD_THREADS, std::max(32, g.tileStride)), smem, s.stream>>>(A);
+    kb<<<g.nTiles, buildThreads, smem, s.stream>>>(A);
     s.prof.total++;
     CK(cudaGetLastError());
     int mc[2] = {0, 0};   // largest list, tile-size overflow
