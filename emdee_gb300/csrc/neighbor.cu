@@ -250,6 +250,44 @@ __global__ void k_sort_cells(const int* start, int nRanks, int* orig, const doub
   }
 }
 
+// The same order for dense cells: one warp per cell; each atom's place is the
+// number of atoms of the cell that precede it in (x key, atom index) order.
+// Cells of more than 32 atoms are sorted by lane 0 as above.
+__global__ void k_sort_cells_warp(const int* start, int nRanks, int* orig, const double* __restrict__ R,
+                                  const int4* __restrict__ atomK, double scale) {
+  const int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (r >= nRanks) return;
+  const int b = start[r], n = start[r + 1] - b;
+  if (n <= 1) return;
+  if (n > 32) {
+    if (lane == 0)
+      for (int i = b + 1; i < b + n; i++) {
+        const int v = orig[i];
+        const float kv = (float)(R[3 * v] * scale - (double)atomK[v].x);
+        int j = i - 1;
+        while (j >= b) {
+          const int u = orig[j];
+          const float ku = (float)(R[3 * u] * scale - (double)atomK[u].x);
+          if (!(ku > kv || (ku == kv && u > v))) break;
+          orig[j + 1] = u;
+          j--;
+        }
+        orig[j + 1] = v;
+      }
+    return;
+  }
+  const int a = lane < n ? orig[b + lane] : 0;
+  const float k = lane < n ? (float)(R[3 * a] * scale - (double)atomK[a].x) : 0.0f;
+  int place = 0;
+  for (int j = 0; j < n; j++) {
+    const int aj = __shfl_sync(0xffffffffu, a, j);
+    const float kj = __shfl_sync(0xffffffffu, k, j);
+    place += (kj < k || (kj == k && aj < a)) ? 1 : 0;
+  }
+  __syncwarp();
+  if (lane < n) orig[b + place] = a;
+}
+
 // per slot: image cell, type, slot of the atom, and the FP32 position and charge
 // (u = M R/L - K, also kept per atom as the build-time reference pos0); per atom
 // the build-time coordinates R0 of the skin check
@@ -687,8 +725,12 @@ static bool build_lists(System& s, bool reuse) {
     CK(cudaGetLastError());
     device_scan(s, g.dCount, g.dStart, g.nRanks);
     k_scatter<<<bl, th, 0, s.stream>>>(g.dAtomK, N, g.dStart, g.dSlotOf, g.dOrig);
-    k_sort_cells<<<(g.nRanks + 255) / 256, 256, 0, s.stream>>>(g.dStart, g.nRanks, g.dOrig, s.dR, g.dAtomK,
-                                                               (double)M / L, g.dKeyX);
+    if (perCell >= 8.0)   // dense cells: a warp per cell
+      k_sort_cells_warp<<<(g.nRanks + 7) / 8, 256, 0, s.stream>>>(g.dStart, g.nRanks, g.dOrig, s.dR, g.dAtomK,
+                                                                  (double)M / L);
+    else
+      k_sort_cells<<<(g.nRanks + 255) / 256, 256, 0, s.stream>>>(g.dStart, g.nRanks, g.dOrig, s.dR, g.dAtomK,
+                                                                 (double)M / L, g.dKeyX);
     k_fill_slots<<<bl, th, 0, s.stream>>>(g.dOrig, N, g.dAtomK, s.dType, g.dK, g.dType8, g.dSlotOf, s.dR,
                                           s.dCharge, (double)M / L, g.dPos4, g.dPos0, s.dR0);
     int* dMax = g.dTileInfo + 2 * g.nTiles;
