@@ -332,14 +332,14 @@ def run_gpu(args):
 
     # ---- the other workloads: replica batch and rigid water (throughput only) ----
     extra = {}
-    if rank == 0 and not args.no_extra:
+    if rank == 0 and world == 1 and not args.no_extra:   # the other workloads: single-GPU runs only
         extra["lj_replicas_256"] = measure_replicas(lib, emdee_gb300, torch, args.replica_steps)
         extra["water_rigid_4096"] = measure_water(lib, emdee_gb300, torch, args.water_steps)
         if not args.no_hmc:
             extra["hmc_binary_lj_8000x64"] = measure_hmc(lib, torch, args.hmc_iterations, args.hmc_configs)
 
     cpu = None
-    if rank == 0 and not args.no_cpu:
+    if rank == 0 and world == 1 and not args.no_cpu:   # the CPU sample: rank 0 at N = 1 only
         rate, threads, n, t = cpu_rate(W, budget_s=20.0, max_steps=100)
         cpu = {"value": rate, "unit": "atom-steps/s", "cores": threads, "kind": "port",
                "sample": "%d velocity-Verlet steps of the full %d-atom box after 1 warm-up step (%.1f s)"
