@@ -829,8 +829,8 @@ static bool build_lists(System& s, bool reuse) {
                              : (A.minimg ? k_build<false, true, true> : k_build<false, false, true>))
                   : (general ? (A.minimg ? k_build<true, true, false> : k_build<true, false, false>)
                              : (A.minimg ? k_build<false, true, false> : k_build<false, false, false>));
-  const int buildThreads = split ? std::min(BUILD_THREADS_SPLIT, g.tileStride * A.tpa)
-                                 : std::min(BUILD_THREADS, std::max(32, g.tileStride));
+  const int buildThreads = std::max(halo_min_threads(geo), split ? std::min(BUILD_THREADS_SPLIT, g.tileStride * A.tpa)
+                                                                 : std::min(BUILD_THREADS, std::max(32, g.tileStride)));
   CK(cudaFuncSetAttribute(kb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
 #ifdef EMDEE_MAX_CARVEOUT
   CK(cudaFuncSetAttribute(kb, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared));

@@ -260,8 +260,9 @@ void device_pair_forces_mixed(System& s, bool compute, bool useInRc, double rc2s
   A.tpa = tpa;
   A.tpaShift = shift;
   static const int thEnv = getenv("EMDEE_PAIR_THREADS") ? atoi(getenv("EMDEE_PAIR_THREADS")) : 0;
-  const int th = thEnv >= 32 && thEnv % 32 == 0 ? std::min(thEnv, maxTh)
-                                                 : std::min(maxTh, std::max(32, g.tileStride * tpa));
+  const int th = std::max(halo_min_threads(A.g), thEnv >= 32 && thEnv % 32 == 0
+                                                     ? std::min(thEnv, maxTh)
+                                                     : std::min(maxTh, std::max(32, g.tileStride * tpa)));
   const int nt = g.nTiles;
   if (variant == 0) {
     const int mod = s.P(0, 0, s.layer - 1).model.p.modifier;

@@ -98,6 +98,10 @@ __device__ int block_exclusive_scan(int* data, int n, int* warpSums) {
   return total;
 }
 
+// The halo scans below need blockDim.x * 8 >= haloCells: launch sites size their
+// blocks with halo_min_threads.
+__host__ __device__ __forceinline__ int halo_min_threads(const TileGeom& g) { return (g.haloCells + 255) / 256 * 32; }
+
 // off[h] = first halo index of halo cell h of tile t; off[haloCells] = halo size.
 __device__ __forceinline__ int halo_offsets(const TileGeom& g, int t, const int* start, int* off, int* ws) {
   for (int h = threadIdx.x; h < g.haloCells; h += blockDim.x) {
