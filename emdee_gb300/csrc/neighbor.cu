@@ -365,8 +365,13 @@ __global__ void k_pack_mixed(const double* __restrict__ R, const double* __restr
 // displacement since the build rounded to FP32 and scaled in FP32 (one FP64
 // subtraction and conversion per coordinate instead of the FP64 M R/L - K).
 // The fused step kernel packs with the same arithmetic.
+__device__ __forceinline__ float d2f(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return d2f_normal(b) ? __uint_as_float(d2f_bits(b)) : (float)x;
+}
+
 __device__ __forceinline__ float4 pack_delta(float4 p0, double dx, double dy, double dz, float scale) {
-  return make_float4(fmaf((float)dx, scale, p0.x), fmaf((float)dy, scale, p0.y), fmaf((float)dz, scale, p0.z), p0.w);
+  return make_float4(fmaf(d2f(dx), scale, p0.x), fmaf(d2f(dy), scale, p0.y), fmaf(d2f(dz), scale, p0.z), p0.w);
 }
 
 __global__ void k_pack_delta(const double* __restrict__ R, const double* __restrict__ R0, const int* orig,

@@ -12,6 +12,8 @@
 
 #include <cstdint>
 
+#include "fpconv.h"
+
 namespace emdee {
 
 struct TileGeom {
