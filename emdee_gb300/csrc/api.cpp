@@ -592,7 +592,7 @@ void EmDee_destroy(tEmDee* md) {
   cudaFree(g.dCount); cudaFree(g.dStart); cudaFree(g.dScanTmp); cudaFree(g.dOrig);
   cudaFree(g.dSelf); cudaFree(g.dK); cudaFree(g.dAtomK); cudaFree(g.dPos4); cudaFree(g.dType8);
   cudaFree(g.dRs64); cudaFree(g.dNb); cudaFree(g.dHaloTab); cudaFree(g.dNbCount); cudaFree(g.dNbInner); cudaFree(g.dTileInfo);
-  cudaFree(g.dSlotOf); cudaFree(g.dPos0); cudaFree(g.dKeyX);
+  cudaFree(g.dSlotOf); cudaFree(g.dPos0); cudaFree(g.dKeyX); cudaFree(g.dLayout);
   cudaFree(s->models.d64); cudaFree(s->models.d32); cudaFree(s->models.coul64); cudaFree(s->models.coul32);
   cudaFree(s->models.interact);
   cudaFree(s->dPartials);

@@ -443,6 +443,7 @@ struct BuildArgs {
   uint16_t* selfIdx;
   int cap, tileStride;
   int tpa, tpaShift;   // threads per atom of the split build (a power of 2) and its log2
+  int* layout;         // out: per tile off[0..haloCells] and cst[0..haloCells-1] (halo_layout_saved)
   int* maxCount;
 };
 
@@ -510,6 +511,11 @@ __global__ void BUILD_BOUNDS k_build(BuildArgs A) {
       if (threadIdx.x == 0) atomicOr(A.maxCount + 1, 1);
       return;
     }
+  }
+  {   // the layout, saved for the force kernels until the next build
+    int* dst = A.layout + (size_t)t * (2 * g.haloCells + 1);
+    for (int h = threadIdx.x; h <= g.haloCells; h += blockDim.x) dst[h] = off[h];
+    for (int h = threadIdx.x; h < g.haloCells; h += blockDim.x) dst[g.haloCells + 1 + h] = cst[h];
   }
   stage_frame(g, off, cst, hxyz, A.pos4, hpos, hslot, single ? (uint8_t*)nullptr : htype, A.type8);
   __syncthreads();
@@ -813,6 +819,8 @@ static bool build_lists(System& s, bool reuse) {
   A.selfIdx = g.dSelf;
   A.tileStride = g.tileStride;
   A.maxCount = g.dTileInfo + 2 * g.nTiles + 2;
+  grow(g.dLayout, g.layoutCap, (size_t)g.nTiles * (2 * g.haloCells + 1));
+  A.layout = g.dLayout;
   size_t smem = build_smem(g, s.ntypes);
   const bool general = s.ntypes > 1 || A.hasBodies || A.hasEx || A.layered;
   // Threads per atom: a system too small to fill the GPU with one thread per atom and

@@ -35,6 +35,7 @@ static const int PAIR_THREADS_GENERAL = 1024;
 struct PairArgsF {
   TileGeom g;
   const int2* tab;
+  const int* layout;   // halo layout saved by the list build
   const float4* pos4;
   const uint8_t* type8;
   const int* start;
@@ -84,7 +85,7 @@ __global__ void PAIR_BOUNDS k_pair_mixed(PairArgsF A) {
     hpos[A.haloCap] = make_float4(1e9f, 1e9f, 1e9f, 0.f);
     if (VAR == 1) htype[A.haloCap] = 0;
   }
-  halo_layout(g, t, A.tab, A.start, off, cst, hxyz, ws);
+  halo_layout_saved(g, t, A.layout, off, cst, hxyz);
   stage_frame(g, off, cst, hxyz, A.pos4, hpos, (int*)nullptr, VAR == 1 ? htype : (uint8_t*)nullptr, A.type8);
   __syncthreads();
 
@@ -218,6 +219,7 @@ void device_pair_forces_mixed(System& s, bool compute, bool useInRc, double rc2s
   PairArgsF A;
   A.g = make_geom(g.M, g.TB);
   A.tab = g.dHaloTab;
+  A.layout = g.dLayout;
   A.pos4 = g.dPos4;
   A.type8 = g.dType8;
   A.start = g.dStart;

@@ -145,6 +145,8 @@ struct Grid {
   int *dNbCount = nullptr, *dNbInner = nullptr;
   int* dTileInfo = nullptr;   // per tile: atoms, halo atoms
   int2* dHaloTab = nullptr;   // per tile and halo cell: rank, packed halo coordinates
+  int* dLayout = nullptr;      // per tile: halo offsets and first slots of the last build
+  size_t layoutCap = 0;
   size_t haloTabCap = 0;
   int tabM = 0, tabTB = 0;    // geometry the halo table was written for
   GridCaps caps;

@@ -144,6 +144,21 @@ __device__ __forceinline__ int halo_layout(const TileGeom& g, int t, const int2*
   return total;
 }
 
+// Halo layout of tile t as written by the list build (layout: per tile
+// 2 haloCells + 1 ints: off[0..haloCells], then cst[0..haloCells-1]); hxyz from
+// the halo cell index.  Ends with a barrier.
+__device__ __forceinline__ int halo_layout_saved(const TileGeom& g, int t, const int* layout, int* off, int* cst,
+                                                 int* hxyz) {
+  const int* src = layout + (size_t)t * (2 * g.haloCells + 1);
+  for (int h = threadIdx.x; h <= g.haloCells; h += blockDim.x) off[h] = src[h];
+  for (int h = threadIdx.x; h < g.haloCells; h += blockDim.x) {
+    cst[h] = src[g.haloCells + 1 + h];
+    if (hxyz) hxyz[h] = (h % g.HW) | (((h / g.HW) % g.HW) << 8) | ((h / (g.HW * g.HW)) << 16);
+  }
+  __syncthreads();
+  return off[g.haloCells];
+}
+
 // Stages the halo of tile t in the tile frame, one thread per halo cell: the
 // cell-local positions of pos4 (cell units) plus the halo cell's offset from the
 // frame origin (halo cell C, C, C).  Optionally records slots and types.
