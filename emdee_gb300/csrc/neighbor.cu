@@ -143,22 +143,55 @@ bool device_skin_check(System& s) {
 // binning (src/neighbor_lists.f90:122-128) and tile sort
 // ---------------------------------------------------------------------------------
 
-__global__ void k_assign(const double* __restrict__ R, int N, double invL, TileGeom g, int4* atomK, int* count,
-                         int* inCell) {
+// FP32 rounding of a double (nearest even) on the integer pipes when the result
+// is a normal float, else the hardware conversion
+__device__ __forceinline__ float d2f(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return d2f_normal(b) ? __uint_as_float(d2f_bits(b)) : (float)x;
+}
+
+// value of an integer-valued double with |f| < 2^31, from its bits (no FP64 pipe)
+__device__ __forceinline__ int dint_exact(double f) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(f);
+  const int e = (int)((b >> 52) & 0x7FF) - 1023;
+  if (e < 0) return 0;
+  const int v = (int)(((b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull) >> (52 - e));
+  return (b >> 63) ? -v : v;
+}
+
+// FP32 copy of a charge, zero below the reference's threshold (|q| > epsilon,
+// src/EmDeeCode.f90:879-880), compared and converted on the integer pipes
+__device__ __forceinline__ float charge_f32(double q) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(q) & 0x7FFFFFFFFFFFFFFFull;
+  return b > 0x3CB0000000000000ull ? d2f(q) : 0.0f;   // 0x3CB0... = 2^-52
+}
+
+// Per atom (API order): the image-resolved cell K = floor(M R / L) of each
+// coordinate, the cell's rank, the cell-local FP32 position u = M R/L - K with the
+// charge (the build-time reference pos0 of the packing), the coordinates R0 of
+// this build for the skin check, and the atom's place among its cell's atoms.
+// M R/L is one FP64 product per coordinate; its floor and remainder are the only
+// other FP64 operations (the remainder is exact), and every later stage of the
+// build reads u instead of recomputing it.  A cell index that differs from the
+// reference's int(M (R/L - floor(R/L))) by rounding at a cell boundary changes
+// only the order of candidates, not the pair set.
+__global__ void k_assign(const double* __restrict__ R, const double* __restrict__ charge, int N, double scale,
+                         TileGeom g, int4* atomK, int* count, int* inCell, float4* pos0, double* __restrict__ R0) {
   int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= N) return;
   int c[3], K[3];
+  float u[3];
   for (int d = 0; d < 3; d++) {
-    // R * (1/L): a cell index that differs from the reference's R / L by an ulp at a
-    // cell boundary changes only the order of candidates, not the pair set
-    double rs = R[3 * a + d] * invL, fl = floor(rs);
-    int ci = (int)(g.M * (rs - fl));
-    ci = ci < 0 ? 0 : (ci >= g.M ? g.M - 1 : ci);   // M*(x - floor x) may round up to M
-    c[d] = ci;
-    K[d] = (int)fl * g.M + ci;
+    const double r = R[3 * a + d], t = r * scale, fl = floor(t);
+    K[d] = dint_exact(fl);
+    int ci = K[d] % g.M;
+    c[d] = ci < 0 ? ci + g.M : ci;
+    u[d] = d2f(t - fl);
+    R0[3 * a + d] = r;
   }
   int rank = cell_rank(g, c[0], c[1], c[2]);
   atomK[a] = make_int4(K[0], K[1], K[2], rank);
+  pos0[a] = make_float4(u[0], u[1], u[2], charge_f32(charge[a]));
   // one atomic per distinct cell of the warp (neighbouring atoms often share a
   // cell); each atom keeps its place among the cell's atoms for the scatter
   const unsigned active = __activemask();
@@ -224,19 +257,15 @@ __global__ void k_scatter(const int4* atomK, int N, const int* start, const int*
   orig[start[atomK[a].w] + inCell[a]] = a;
 }
 
-// Order inside a cell: ascending cell-local x coordinate u.x (computed as in
-// k_fill_slots, so the build's staged positions are sorted along x within
-// every cell and hence along every stencil row), ties by ascending atom index.
-// Deterministic for given coordinates.
-__global__ void k_sort_cells(const int* start, int nRanks, int* orig, const double* __restrict__ R,
-                             const int4* __restrict__ atomK, double scale, float* key) {
+// Order inside a cell: ascending cell-local x coordinate u.x (pos0 of k_assign,
+// so the build's staged positions are sorted along x within every cell and hence
+// along every stencil row), ties by ascending atom index.  Deterministic for
+// given coordinates.
+__global__ void k_sort_cells(const int* start, int nRanks, int* orig, const float4* __restrict__ pos0, float* key) {
   int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= nRanks) return;
   int b = start[r], e = start[r + 1];
-  for (int i = b; i < e; i++) {
-    int a = orig[i];
-    key[i] = (float)(R[3 * a] * scale - (double)atomK[a].x);
-  }
+  for (int i = b; i < e; i++) key[i] = pos0[orig[i]].x;
   for (int i = b + 1; i < e; i++) {
     int v = orig[i], j = i - 1;
     float kv = key[i];
@@ -253,8 +282,7 @@ __global__ void k_sort_cells(const int* start, int nRanks, int* orig, const doub
 // The same order for dense cells: one warp per cell; each atom's place is the
 // number of atoms of the cell that precede it in (x key, atom index) order.
 // Cells of more than 32 atoms are sorted by lane 0 as above.
-__global__ void k_sort_cells_warp(const int* start, int nRanks, int* orig, const double* __restrict__ R,
-                                  const int4* __restrict__ atomK, double scale) {
+__global__ void k_sort_cells_warp(const int* start, int nRanks, int* orig, const float4* __restrict__ pos0) {
   const int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (r >= nRanks) return;
   const int b = start[r], n = start[r + 1] - b;
@@ -263,11 +291,11 @@ __global__ void k_sort_cells_warp(const int* start, int nRanks, int* orig, const
     if (lane == 0)
       for (int i = b + 1; i < b + n; i++) {
         const int v = orig[i];
-        const float kv = (float)(R[3 * v] * scale - (double)atomK[v].x);
+        const float kv = pos0[v].x;
         int j = i - 1;
         while (j >= b) {
           const int u = orig[j];
-          const float ku = (float)(R[3 * u] * scale - (double)atomK[u].x);
+          const float ku = pos0[u].x;
           if (!(ku > kv || (ku == kv && u > v))) break;
           orig[j + 1] = u;
           j--;
@@ -277,7 +305,7 @@ __global__ void k_sort_cells_warp(const int* start, int nRanks, int* orig, const
     return;
   }
   const int a = lane < n ? orig[b + lane] : 0;
-  const float k = lane < n ? (float)(R[3 * a] * scale - (double)atomK[a].x) : 0.0f;
+  const float k = lane < n ? pos0[a].x : 0.0f;
   int place = 0;
   for (int j = 0; j < n; j++) {
     const int aj = __shfl_sync(0xffffffffu, a, j);
@@ -289,29 +317,16 @@ __global__ void k_sort_cells_warp(const int* start, int nRanks, int* orig, const
 }
 
 // per slot: image cell, type, slot of the atom, and the FP32 position and charge
-// (u = M R/L - K, also kept per atom as the build-time reference pos0); per atom
-// the build-time coordinates R0 of the skin check
+// (pos0 of k_assign)
 __global__ void k_fill_slots(const int* orig, int N, const int4* atomK, const int* type, int4* K, uint8_t* type8,
-                             int* slotOf, const double* __restrict__ R, const double* __restrict__ charge,
-                             double scale, float4* pos4, float4* pos0, double* __restrict__ R0) {
+                             int* slotOf, const float4* __restrict__ pos0, float4* pos4) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= N) return;
   int a = orig[s];
-  const int4 k = atomK[a];
-  K[s] = k;
+  K[s] = atomK[a];
   slotOf[a] = s;
   type8[s] = (uint8_t)(type[a] - 1);
-  const double rx = R[3 * a], ry = R[3 * a + 1], rz = R[3 * a + 2];
-  float ux = (float)(rx * scale - (double)k.x);
-  float uy = (float)(ry * scale - (double)k.y);
-  float uz = (float)(rz * scale - (double)k.z);
-  double q = charge[a];
-  const float4 v = make_float4(ux, uy, uz, fabs(q) > 2.220446049250313e-16 ? (float)q : 0.0f);
-  pos4[s] = v;
-  pos0[a] = v;
-  R0[3 * a] = rx;   // the positions of this build, for the skin check
-  R0[3 * a + 1] = ry;
-  R0[3 * a + 2] = rz;
+  pos4[s] = pos0[a];
 }
 
 __global__ void k_halo_table(TileGeom g, int2* tab) {
@@ -363,13 +378,8 @@ __global__ void k_pack_mixed(const double* __restrict__ R, const double* __restr
 
 // Between builds, with the box of the last build: u = u0 + (R - R0) M/L, the
 // displacement since the build rounded to FP32 and scaled in FP32 (one FP64
-// subtraction and conversion per coordinate instead of the FP64 M R/L - K).
-// The fused step kernel packs with the same arithmetic.
-__device__ __forceinline__ float d2f(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  return d2f_normal(b) ? __uint_as_float(d2f_bits(b)) : (float)x;
-}
-
+// subtraction per coordinate instead of the FP64 M R/L - K).  The fused step
+// kernel packs with the same arithmetic.
 __device__ __forceinline__ float4 pack_delta(float4 p0, double dx, double dy, double dz, float scale) {
   return make_float4(fmaf(d2f(dx), scale, p0.x), fmaf(d2f(dy), scale, p0.y), fmaf(d2f(dz), scale, p0.z), p0.w);
 }
@@ -517,7 +527,7 @@ __global__ void BUILD_BOUNDS k_build(BuildArgs A) {
     for (int h = threadIdx.x; h <= g.haloCells; h += blockDim.x) dst[h] = off[h];
     for (int h = threadIdx.x; h < g.haloCells; h += blockDim.x) dst[g.haloCells + 1 + h] = cst[h];
   }
-  stage_frame(g, off, cst, hxyz, A.pos4, hpos, hslot, single ? (uint8_t*)nullptr : htype, A.type8);
+  stage_frame_flat(g, off, cst, hxyz, A.pos4, hpos, hslot, single ? (uint8_t*)nullptr : htype, A.type8);
   __syncthreads();
   const bool none = A.ntypes == 1 && !sinter[0];   // the only type pair does not interact: empty lists
   const bool filterByAtom = GENERAL && (A.hasBodies || A.hasEx);
@@ -569,28 +579,49 @@ __global__ void BUILD_BOUNDS k_build(BuildArgs A) {
         xhi = pi.x + w;
         while (q < q1 && hpos[q].x <= xlo) q++;
       }
-      for (; q < q1; q++) {
-        const float4 pj = hpos[q];
-        if (!MINIMG && pj.x >= xhi) break;
-        float ex = pi.x - pj.x, ey = pi.y - pj.y, ez = pi.z - pj.z;
-        if (MINIMG) {
-          ex -= A.Mf * rintf(ex / A.Mf);
-          ey -= A.Mf * rintf(ey / A.Mf);
-          ez -= A.Mf * rintf(ez / A.Mf);
+      // candidates in groups of CG: the loads and distance tests of a group are
+      // independent (predicated, no branch per candidate), then the accepted ones
+      // are taken in ascending order; a group that reaches the row's end or the
+      // window's end is the last (the row is sorted along x)
+      constexpr int CG = 2;   // pairs: measured faster than single candidates or groups of four
+      for (; q < q1; q += CG) {
+        float4 pj[CG];
+#pragma unroll
+        for (int u = 0; u < CG; u++) pj[u] = hpos[min(q + u, q1 - 1)];
+        float r2s[CG];
+        unsigned cand = 0;
+        bool last = false;
+#pragma unroll
+        for (int u = 0; u < CG; u++) {
+          const bool valid = q + u < q1 && (MINIMG || pj[u].x < xhi);
+          last |= !valid;
+          float ex = pi.x - pj[u].x, ey = pi.y - pj[u].y, ez = pi.z - pj[u].z;
+          if (MINIMG) {
+            ex -= A.Mf * rintf(ex / A.Mf);
+            ey -= A.Mf * rintf(ey / A.Mf);
+            ez -= A.Mf * rintf(ez / A.Mf);
+          }
+          r2s[u] = ex * ex + ey * ey + ez * ez;
+          cand |= (valid && r2s[u] < A.hi2 && q + u != myq) ? 1u << u : 0u;
         }
-        const float r2 = ex * ex + ey * ey + ez * ez;
-        if (r2 >= A.hi2 || q == myq) continue;
-        if (!(r2 < A.lo2 || exact_inside(A.R, A.L, ai, A.orig[hslot[q]], A.thr))) continue;
-        if (GENERAL && !single && !sinter[ti * A.ntypes + htype[q]]) continue;
-        if (filterByAtom) {
-          const int aj = A.orig[hslot[q]];
-          if (A.hasBodies && A.body[aj] == bi) continue;
-          if (hasEx && excluded(A, ai, aj)) continue;
+#pragma unroll
+        for (int u = 0; u < CG; u++) {
+          if (!((cand >> u) & 1u)) continue;
+          const int qu = q + u;
+          const float r2 = r2s[u];
+          if (!(r2 < A.lo2 || exact_inside(A.R, A.L, ai, A.orig[hslot[qu]], A.thr))) continue;
+          if (GENERAL && !single && !sinter[ti * A.ntypes + htype[qu]]) continue;
+          if (filterByAtom) {
+            const int aj = A.orig[hslot[qu]];
+            if (A.hasBodies && A.body[aj] == bi) continue;
+            if (hasEx && excluded(A, ai, aj)) continue;
+          }
+          bool inner = true;
+          if (layered)
+            inner = r2 < A.loIn2 || (r2 < A.hiIn2 && exact_inside(A.R, A.L, ai, A.orig[hslot[qu]], A.thrIn));
+          f(qu, inner);
         }
-        bool inner = true;
-        if (layered)
-          inner = r2 < A.loIn2 || (r2 < A.hiIn2 && exact_inside(A.R, A.L, ai, A.orig[hslot[q]], A.thrIn));
-        f(q, inner);
+        if (last) break;
       }
     };
     auto put = [&](int k, int q) {
@@ -732,18 +763,17 @@ static bool build_lists(System& s, bool reuse) {
     CK(cudaMemsetAsync(g.dCount, 0, sizeof(int) * (g.nRanks + 1), s.stream));
     s.prof.total += reuse ? 7 : 8;   // assign, 3 scan phases, scatter, sort, fill (, tile info)
     // the slot array holds each atom's place in its cell until k_fill_slots
-    k_assign<<<bl, th, 0, s.stream>>>(s.dR, N, 1.0 / L, geo, g.dAtomK, g.dCount, g.dSlotOf);
+    k_assign<<<bl, th, 0, s.stream>>>(s.dR, s.dCharge, N, (double)M / L, geo, g.dAtomK, g.dCount, g.dSlotOf,
+                                      g.dPos0, s.dR0);
     CK(cudaGetLastError());
     device_scan(s, g.dCount, g.dStart, g.nRanks);
     k_scatter<<<bl, th, 0, s.stream>>>(g.dAtomK, N, g.dStart, g.dSlotOf, g.dOrig);
     if (perCell >= 8.0)   // dense cells: a warp per cell
-      k_sort_cells_warp<<<(g.nRanks + 7) / 8, 256, 0, s.stream>>>(g.dStart, g.nRanks, g.dOrig, s.dR, g.dAtomK,
-                                                                  (double)M / L);
+      k_sort_cells_warp<<<(g.nRanks + 7) / 8, 256, 0, s.stream>>>(g.dStart, g.nRanks, g.dOrig, g.dPos0);
     else
-      k_sort_cells<<<(g.nRanks + 255) / 256, 256, 0, s.stream>>>(g.dStart, g.nRanks, g.dOrig, s.dR, g.dAtomK,
-                                                                 (double)M / L, g.dKeyX);
-    k_fill_slots<<<bl, th, 0, s.stream>>>(g.dOrig, N, g.dAtomK, s.dType, g.dK, g.dType8, g.dSlotOf, s.dR,
-                                          s.dCharge, (double)M / L, g.dPos4, g.dPos0, s.dR0);
+      k_sort_cells<<<(g.nRanks + 255) / 256, 256, 0, s.stream>>>(g.dStart, g.nRanks, g.dOrig, g.dPos0, g.dKeyX);
+    k_fill_slots<<<bl, th, 0, s.stream>>>(g.dOrig, N, g.dAtomK, s.dType, g.dK, g.dType8, g.dSlotOf, g.dPos0,
+                                          g.dPos4);
     int* dMax = g.dTileInfo + 2 * g.nTiles;
     CK(cudaMemsetAsync(dMax, 0, sizeof(int) * 4, s.stream));
     if (reuse) break;
@@ -865,7 +895,7 @@ static bool build_lists(System& s, bool reuse) {
     if (mc[0] > 65528) fatal("neighbor list build", "more than 65528 neighbors for one atom");
     g.cap = std::min(65528, (mc[0] + mc[0] / 8 + 16 + 7) / 8 * 8);
   }
-  s.r0Valid = true;   // R0 was written by k_fill_slots
+  s.r0Valid = true;   // R0 was written by k_assign
   s.builtL = L;
   return true;
 }

@@ -86,7 +86,7 @@ __global__ void PAIR_BOUNDS k_pair_mixed(PairArgsF A) {
     if (VAR == 1) htype[A.haloCap] = 0;
   }
   halo_layout_saved(g, t, A.layout, off, cst, hxyz);
-  stage_frame(g, off, cst, hxyz, A.pos4, hpos, (int*)nullptr, VAR == 1 ? htype : (uint8_t*)nullptr, A.type8);
+  stage_frame_flat(g, off, cst, hxyz, A.pos4, hpos, (int*)nullptr, VAR == 1 ? htype : (uint8_t*)nullptr, A.type8);
   __syncthreads();
 
   NBParams<float> m0 = A.table[0].model;

@@ -37,11 +37,21 @@ __device__ __forceinline__ void grid_reduce_lane0(const double (&v)[NQ], double*
 #pragma unroll
   for (int q = 0; q < NQ; q++) {
     double s = 0.0, c = 0.0;
-    for (unsigned int b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
-      double x = __ldcg(&partials[(size_t)b * NQ + q]);
-      double t = s + x;
-      c += fabs(s) >= fabs(x) ? (s - t) + x : (x - t) + s;
-      s = t;
+    constexpr int U = 8;   // partials in flight per thread, added in increasing block order
+    for (unsigned int b0 = threadIdx.x; b0 < gridDim.x; b0 += U * blockDim.x) {
+      double xs[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const unsigned int b = b0 + u * blockDim.x;
+        xs[u] = b < gridDim.x ? __ldcg(&partials[(size_t)b * NQ + q]) : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        if (b0 + u * blockDim.x >= gridDim.x) break;
+        const double x = xs[u], t = s + x;
+        c += fabs(s) >= fabs(x) ? (s - t) + x : (x - t) + s;
+        s = t;
+      }
     }
     double x = s + c;
 #pragma unroll
@@ -170,13 +180,24 @@ __device__ __forceinline__ void grid_reduce_ff(const float (&v)[NQ], float2* par
     hi[q] = 0.f;
     lo[q] = 0.f;
   }
-  for (unsigned int b = threadIdx.x; b < gridDim.x; b += blockDim.x)
+  // U partials per quantity in flight per thread, added in increasing block order
+  constexpr int U = 8;
+  for (unsigned int b0 = threadIdx.x; b0 < gridDim.x; b0 += U * blockDim.x) {
+    float2 x[U][NQ];
 #pragma unroll
-    for (int q = 0; q < NQ; q++) {
-      if (!((MASK >> q) & 1u)) continue;
-      const float2 x = __ldcg(&partials[(size_t)b * NQ + q]);
-      ff_add(hi[q], lo[q], x.x, x.y);
+    for (int u = 0; u < U; u++) {
+      const unsigned int b = b0 + u * blockDim.x;
+#pragma unroll
+      for (int q = 0; q < NQ; q++)
+        if ((MASK >> q) & 1u) x[u][q] = b < gridDim.x ? __ldcg(&partials[(size_t)b * NQ + q]) : make_float2(0.f, 0.f);
     }
+#pragma unroll
+    for (int u = 0; u < U; u++)
+      if (b0 + u * blockDim.x < gridDim.x)
+#pragma unroll
+        for (int q = 0; q < NQ; q++)
+          if ((MASK >> q) & 1u) ff_add(hi[q], lo[q], x[u][q].x, x[u][q].y);
+  }
   warp_sum_ff<NQ, MASK>(hi, lo);
   if (lane == 0)
 #pragma unroll

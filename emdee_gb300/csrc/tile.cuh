@@ -184,6 +184,49 @@ __device__ __forceinline__ void stage_frame(const TileGeom& g, const int* off, c
   }
 }
 
+// Stages the halo of tile t in the tile frame with one thread per halo atom (the
+// loads of a warp cover consecutive slots of cell runs, several in flight per
+// thread).  A first pass records each halo index's cell in the x word of its
+// hpos entry, which the thread staging that entry then overwrites.  Needs the
+// layout in shared memory behind a barrier; ends without one.  Optionally
+// records slots and types.
+__device__ __forceinline__ void stage_frame_flat(const TileGeom& g, const int* off, const int* cst, const int* hxyz,
+                                                 const float4* pos4, float4* hpos, int* hslot, uint8_t* htype,
+                                                 const uint8_t* type8) {
+  int* hcell = reinterpret_cast<int*>(hpos);
+  for (int h = threadIdx.x; h < g.haloCells; h += blockDim.x)
+    for (int k = off[h], e = off[h + 1]; k < e; k++) hcell[4 * k] = h;
+  __syncthreads();
+  const int n = off[g.haloCells];
+  constexpr int U = 4;
+  for (int k0 = threadIdx.x; k0 < n; k0 += U * blockDim.x) {
+    float4 p[U];
+    int hh[U], slot[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int k = k0 + u * blockDim.x;
+      if (k < n) {
+        const int h = hcell[4 * k];
+        hh[u] = h;
+        slot[u] = cst[h] + k - off[h];
+        p[u] = pos4[slot[u]];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int k = k0 + u * blockDim.x;
+      if (k < n) {
+        const int c = hxyz[hh[u]];
+        const float fx = (float)((c & 255) - g.C), fy = (float)(((c >> 8) & 255) - g.C),
+                    fz = (float)((c >> 16) - g.C);
+        hpos[k] = make_float4(p[u].x + fx, p[u].y + fy, p[u].z + fz, p[u].w);
+        if (hslot) hslot[k] = slot[u];
+        if (htype) htype[k] = type8[slot[u]];
+      }
+    }
+  }
+}
+
 // Exact float -> double conversion with integer operations (normal numbers and
 // zero; denormals were flushed by the FP32 arithmetic).  Keeps the FP64 pipe,
 // which is slow on this GPU, out of the force stores.
