@@ -68,7 +68,9 @@ struct PairArgsF {
 // wrap would bring the sentinel back).
 template <bool COMPUTE, int VAR, int MOD, bool MINIMG, bool COUNT>
 __global__ void PAIR_BOUNDS k_pair_mixed(PairArgsF A) {
-  if (A.skip != nullptr && *A.skip != 0.0) return;
+  // the flag is 0.0 or 1.0: tested on its bits (an FP64 compare in every thread of
+  // every block would queue on the slow FP64 pipe)
+  if (A.skip != nullptr && __double_as_longlong(*A.skip) != 0) return;
   extern __shared__ __align__(16) unsigned char sraw[];
   __shared__ int ws[33];
   const TileGeom g = A.g;
