@@ -309,7 +309,13 @@ static void compute_forces_impl(tEmDee* md) {
     s.hResult[9] = 1.0;
   }
   if (rebuild) {
-    device_build_lists(s);
+    if (two_level_active(s) && s.pairs_exist[s.layer - 1]) {
+      // the filtering launch computes this step's forces as well
+      device_rebuild_two_level(s, compute);
+      forcesDone = true;
+    } else {
+      device_build_lists(s);
+    }
     md->Builds++;
   }
   double t1 = wtime();
@@ -532,6 +538,7 @@ tEmDee EmDee_system(int threads, int layers, double rc, double skin, int N, int*
     if (s->nfree > 0) CK(cudaMemcpy(s->dFree, s->freeList.data(), sizeof(int) * s->nfree, cudaMemcpyHostToDevice));
   }
   CK(cudaMallocHost(&s->hResult, sizeof(double) * 48));
+  CK(cudaMallocHost(&s->hFlags, sizeof(int) * 16));
   CK(cudaMalloc(&s->dResult, sizeof(double) * 48));
   CK(cudaMalloc(&s->dTicket, sizeof(unsigned int) * 8));
   CK(cudaMemset(s->dTicket, 0, sizeof(unsigned int) * 8));
@@ -555,6 +562,13 @@ void EmDee_set_precision(tEmDee md, int mode) {
   if (mode != 0 && mode != 1) fatal("precision setting", "mode must be 0 (mixed) or 1 (fp64)");
   s.precision = mode;
 }
+
+void EmDee_set_outer_skin(tEmDee md, double delta) {
+  System& s = *sys_of(md);
+  s.outerSkin = delta < 0.0 ? -1.0 : delta;
+}
+
+long EmDee_outer_builds(tEmDee md) { return sys_of(md)->outerBuilds; }
 
 void EmDee_destroy(tEmDee* md) {
   System* s = sys_of(*md);
@@ -593,6 +607,7 @@ void EmDee_destroy(tEmDee* md) {
   cudaFree(g.dSelf); cudaFree(g.dK); cudaFree(g.dAtomK); cudaFree(g.dPos4); cudaFree(g.dType8);
   cudaFree(g.dRs64); cudaFree(g.dNb); cudaFree(g.dHaloTab); cudaFree(g.dNbCount); cudaFree(g.dNbInner); cudaFree(g.dTileInfo);
   cudaFree(g.dSlotOf); cudaFree(g.dPos0); cudaFree(g.dKeyX); cudaFree(g.dLayout);
+  cudaFree(g.dNbOuter); cudaFree(g.dNbCountOuter); cudaFree(g.dROuter);
   cudaFree(s->models.d64); cudaFree(s->models.d32); cudaFree(s->models.coul64); cudaFree(s->models.coul32);
   cudaFree(s->models.interact);
   cudaFree(s->dPartials);
@@ -600,6 +615,7 @@ void EmDee_destroy(tEmDee* md) {
   cudaFree(s->dTicket);
   cudaFree(s->dResult);
   cudaFreeHost(s->hResult);
+  cudaFreeHost(s->hFlags);
   cudaFreeHost(s->hMirrorR); cudaFreeHost(s->hMirrorP); cudaFreeHost(s->hMirrorF); cudaFreeHost(s->hMirrorLayerF);
   if (s->ownsLbox) delete s->Lbox;
   cudaStreamDestroy(s->stream);

@@ -147,6 +147,13 @@ void flush_pending(System& s) {
 
 // Chooses the force kernel for the current layer and leaves the four sums in
 // hResult[0..3] (src/EmDeeData.f90:644-685).
+// single-type Lennard-Jones without charges takes the specialised kernel
+bool pair_lj_only(System& s) {
+  const int l = s.layer - 1;
+  return s.ntypes == 1 && s.P(0, 0, l).model.kind == MK_LJ_CUT &&
+         !(s.P(0, 0, l).coulomb && s.coul[l].kind != MK_COUL_NONE);
+}
+
 bool device_pair_forces(System& s, bool compute, bool speculative) {
   const int l = s.layer - 1;
   const double L = *s.Lbox, invL2 = 1.0 / (L * L);
@@ -167,11 +174,8 @@ bool device_pair_forces(System& s, bool compute, bool speculative) {
   if (s.precision == 1) {
     device_pair_forces_fp64(s, compute, useInRc, rc2);
   } else {
-    // single-type Lennard-Jones without charges takes the specialised kernel
-    bool lj_only = s.ntypes == 1 && s.P(0, 0, l).model.kind == MK_LJ_CUT &&
-                   !(s.P(0, 0, l).coulomb && s.coul[l].kind != MK_COUL_NONE);
     s.pairSkip = speculative ? s.dResult + 9 : nullptr;
-    device_pair_forces_mixed(s, compute, useInRc, rc2, lj_only ? 0 : 1);
+    device_pair_forces_mixed(s, compute, useInRc, rc2, pair_lj_only(s) ? 0 : 1);
     s.pairSkip = nullptr;
   }
   prof_end(s, PK_PAIR);

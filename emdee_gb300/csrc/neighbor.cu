@@ -24,7 +24,7 @@
 namespace emdee {
 
 static const int NDIV = 2;   // src/EmDeeData.f90:33
-static const double BAND = 4e-5;
+static const double BAND = LIST_BAND;
 
 // ---------------------------------------------------------------------------------
 // skin check: maximum_approach_sq (src/neighbor_lists.f90:41-59)
@@ -457,17 +457,6 @@ struct BuildArgs {
   int* maxCount;
 };
 
-// FP64 minimum-image distance test of src/neighbor_lists.f90:247-250
-__device__ __noinline__ bool exact_inside(const double* R, double L, int a, int b, double thr) {
-  double d[3];
-  for (int k = 0; k < 3; k++) {
-    double x = R[3 * a + k] / L - R[3 * b + k] / L;
-    d[k] = x - round(x);
-  }
-  double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-  return r2 < thr;
-}
-
 __device__ __forceinline__ bool excluded(const BuildArgs& A, int a, int b) {
   int f = A.exFirst[a], n = A.exCount[a];
   for (int k = 0; k < n; k++) {
@@ -711,7 +700,14 @@ static bool build_lists(System& s, bool reuse) {
   GridCaps& c = g.caps;
   const int N = s.natoms;
   const double L = *s.Lbox;
-  int M = (int)std::floor(NDIV * L / s.xRc);
+  // two-level lists: this build writes the outer lists, of radius rc + skin + delta
+  const bool outer = two_level_active(s);
+  const double delta = outer ? outer_delta(s) : 0.0;
+  const double xRc = s.xRc + delta, xRcSq = xRc * xRc;
+  uint16_t*& nbList = outer ? g.dNbOuter : g.dNb;
+  size_t& nbCap = outer ? c.nbOuter : c.nb;
+  int& cap = outer ? g.capOuter : g.cap;
+  int M = (int)std::floor(NDIV * L / xRc);
   M = std::max(M, 2 * NDIV + 1);
   double perCell = (double)N / ((double)M * M * M);
   int TB = choose_tile(M, perCell);
@@ -756,7 +752,7 @@ static bool build_lists(System& s, bool reuse) {
     }
     if (c.tiles < (size_t)g.nTiles) {
       CK(cudaFree(g.dTileInfo));
-      CK(cudaMalloc(&g.dTileInfo, sizeof(int) * (2 * g.nTiles + 4)));
+      CK(cudaMalloc(&g.dTileInfo, sizeof(int) * (2 * g.nTiles + 6)));
       c.tiles = g.nTiles;
     }
     int th = 256, bl = (N + th - 1) / th;
@@ -808,12 +804,19 @@ static bool build_lists(System& s, bool reuse) {
     g.tabTB = g.TB;
   }
   // neighbor capacity: expected full-list count with margin, grown on overflow
-  if (g.cap == 0) {
+  if (cap == 0) {
     double rho = N / (L * L * L);
-    double expected = rho * 4.18879020478639 * s.xRcSq * s.xRc;
-    g.cap = (int)std::min(65528.0, expected * 1.35 + 32);
+    double expected = rho * 4.18879020478639 * xRcSq * xRc;
+    cap = (int)std::min(65528.0, expected * 1.35 + 32);
   }
-  g.cap = (g.cap + 7) / 8 * 8;
+  cap = (cap + 7) / 8 * 8;
+  if (outer && c.outerAtoms < (size_t)N) {
+    CK(cudaFree(g.dNbCountOuter));
+    CK(cudaFree(g.dROuter));
+    CK(cudaMalloc(&g.dNbCountOuter, sizeof(int) * N));
+    CK(cudaMalloc(&g.dROuter, sizeof(double) * 3 * N));
+    c.outerAtoms = N;
+  }
   const double invL2 = 1.0 / (L * L);
   BuildArgs A;
   A.g = geo;
@@ -833,7 +836,7 @@ static bool build_lists(System& s, bool reuse) {
   A.hasEx = s.hasExclusions;
   A.R = s.dR;
   A.L = L;
-  A.thr = s.xRcSq * invL2;    // src/neighbor_lists.f90:213-214
+  A.thr = xRcSq * invL2;    // src/neighbor_lists.f90:213-214 (outer lists: rc + skin + delta)
   A.thrIn = s.xInRcSq * invL2;
   double M2 = (double)g.M * g.M;
   A.lo2 = (float)(A.thr * M2 * (1.0 - BAND));
@@ -844,7 +847,7 @@ static bool build_lists(System& s, bool reuse) {
   A.minimg = g.M == 5 ? 1 : 0;
   A.Mf = (float)g.M;
   A.haloCap = g.maxHalo;
-  A.nbCount = g.dNbCount;
+  A.nbCount = outer ? g.dNbCountOuter : g.dNbCount;
   A.nbInner = g.dNbInner;
   A.selfIdx = g.dSelf;
   A.tileStride = g.tileStride;
@@ -857,7 +860,7 @@ static bool build_lists(System& s, bool reuse) {
   // with long lists (more than 48 entries per thread) splits the stencil rows of each
   // atom over 2, 4 or 8 threads (blocks of up to 1024 threads).
   {
-    const double expected = N / (L * L * L) * 4.18879020478639 * s.xRcSq * s.xRc;
+    const double expected = N / (L * L * L) * 4.18879020478639 * xRcSq * xRc;
     int tpa = 1, shift = 0;
     while (tpa < 8 && g.tileStride * tpa * 2 <= BUILD_THREADS_SPLIT && (double)N * tpa * 2 <= 152.0 * 2048 &&
            expected / (tpa * 2) >= 48) {
@@ -879,10 +882,10 @@ static bool build_lists(System& s, bool reuse) {
   CK(cudaFuncSetAttribute(kb, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared));
 #endif
   for (int attempt = 0; attempt < 3; attempt++) {
-    size_t need = (size_t)g.nTiles * g.cap * g.tileStride;
-    grow(g.dNb, c.nb, need);
-    A.nb = g.dNb;
-    A.cap = g.cap;
+    size_t need = (size_t)g.nTiles * cap * g.tileStride;
+    grow(nbList, nbCap, need);
+    A.nb = nbList;
+    A.cap = cap;
     CK(cudaMemsetAsync(A.maxCount, 0, sizeof(int), s.stream));
     kb<<<g.nTiles, buildThreads, smem, s.stream>>>(A);
     s.prof.total++;
@@ -891,12 +894,18 @@ static bool build_lists(System& s, bool reuse) {
     CK(cudaMemcpyAsync(mc, A.maxCount, 2 * sizeof(int), cudaMemcpyDeviceToHost, s.stream));
     CK(cudaStreamSynchronize(s.stream));
     if (mc[1]) return false;
-    if (mc[0] <= g.cap) break;
+    if (mc[0] <= cap) break;
     if (mc[0] > 65528) fatal("neighbor list build", "more than 65528 neighbors for one atom");
-    g.cap = std::min(65528, (mc[0] + mc[0] / 8 + 16 + 7) / 8 * 8);
+    cap = std::min(65528, (mc[0] + mc[0] / 8 + 16 + 7) / 8 * 8);
   }
   s.r0Valid = true;   // R0 was written by k_assign
   s.builtL = L;
+  s.listsOuter = outer;
+  if (outer) {   // the reference positions of the coverage test
+    CK(cudaMemcpyAsync(g.dROuter, s.dR, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, s.stream));
+    s.outerDelta = delta;
+    s.outerL = L;
+  }
   return true;
 }
 
@@ -904,6 +913,145 @@ void device_build_lists(System& s) {
   prof_begin(s, PK_BUILD);
   if (!build_lists(s, true)) build_lists(s, false);
   prof_end(s, PK_BUILD);
+}
+
+// ---------------------------------------------------------------------------------
+// two-level lists
+// ---------------------------------------------------------------------------------
+//
+// An outer build lists every pair within rc + skin + delta; the force kernel of a
+// rebuild step filters those lists into the lists the reference would build (every
+// pair within rc + skin, the same FP32 + FP64-band test as k_build), as long as
+// the outer lists still hold every such pair: with d1 >= d2 the two largest
+// displacements since the outer build, a pair now within rc + skin was within
+// rc + skin + d1 + d2 then, so d1 + d2 < delta suffices.  The rebuild schedule and
+// the pair sets stay those of the reference; only the work per rebuild changes.
+
+// Off unless requested (EmDee_set_outer_skin, or EMDEE_OUTER_SKIN for systems that
+// did not set it).  Measured on the 1M-atom Lennard-Jones bench (skin 0.3, T* 1.5):
+// the fastest of a million atoms cross any outer skin up to 0.9 within two rebuild
+// periods, so outer builds (1.7x a build at rc + skin + 0.45) come every second
+// rebuild, and the filtering launch costs about as much as the build it replaces:
+// 387 us per step against 350 with single-level lists.  Slower dynamics (more
+// rebuilds per outer build) are where the outer lists pay.
+double outer_delta(System& s) {
+  if (s.outerSkin >= 0.0) return s.outerSkin;
+  static const double env = getenv("EMDEE_OUTER_SKIN") ? atof(getenv("EMDEE_OUTER_SKIN")) : 0.0;
+  return env > 0.0 ? env : 0.0;
+}
+
+bool two_level_active(System& s) {
+  const double d = outer_delta(s);
+  if (!(d > 0.0) || s.precision != 0 || s.nlayers != 1 || !(s.skin > 0.0) || s.xInRcSq < s.xRcSq) return false;
+  if (!pair_lj_only(s)) return false;
+  return (int)std::floor(NDIV * *s.Lbox / (s.xRc + d)) > 2 * NDIV + 1;   // outer cells: M > 5
+}
+
+// Coverage test of the outer lists and start of a new rebuild period: the largest
+// and second largest squared displacement since the outer build (FP64 differences,
+// FP32 squares, compared as non-negative bit patterns, an order-independent pair);
+// result[40] = 0 if d1 + d2 < delta (with a relative margin for the FP32 squares),
+// else 1, result[41] = d1 + d2.  Also R0 = R and pos0 = the current packed position
+// of every atom (the reference positions of the skin check and of the packing).
+__global__ void __launch_bounds__(SKIN_THREADS) k_cover(const double* __restrict__ R, const double* __restrict__ RO,
+                                                        const int* __restrict__ slotOf,
+                                                        const float4* __restrict__ pos4, int N, double delta,
+                                                        double* __restrict__ R0, float4* __restrict__ pos0,
+                                                        int2* partial, unsigned int* ticket, double* result) {
+  __shared__ int2 wsum[SKIN_THREADS / 32];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int a = 0, b = 0;   // bits of the largest and second largest d^2 (FP32, >= 0)
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    float d2 = 0.0f;
+    for (int k = 0; k < 3; k++) {
+      const double r = R[3 * i + k];
+      const float d = d2f(r - RO[3 * i + k]);
+      d2 = fmaf(d, d, d2);
+      R0[3 * i + k] = r;
+    }
+    pos0[i] = pos4[slotOf[i]];
+    const int v = __float_as_int(d2);
+    b = max(b, min(a, v));
+    a = max(a, v);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const int oa = __shfl_down_sync(0xffffffffu, a, o), ob = __shfl_down_sync(0xffffffffu, b, o);
+    b = max(max(b, ob), min(a, oa));
+    a = max(a, oa);
+  }
+  if (lane == 0) wsum[warp] = make_int2(a, b);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int2 t = wsum[0];
+    for (int w = 1; w < SKIN_THREADS / 32; w++) {
+      t.y = max(max(t.y, wsum[w].y), min(t.x, wsum[w].x));
+      t.x = max(t.x, wsum[w].x);
+    }
+    partial[blockIdx.x] = t;
+    __threadfence();
+    last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last || threadIdx.x != 0) return;
+  __threadfence();
+  int2 t = make_int2(0, 0);
+  for (unsigned int k = 0; k < gridDim.x; k++) {
+    const int2 p = __ldcg(&partial[k]);
+    t.y = max(max(t.y, p.y), min(t.x, p.x));
+    t.x = max(t.x, p.x);
+  }
+  const double sum = sqrt((double)__int_as_float(t.x)) + sqrt((double)__int_as_float(t.y));
+  result[41] = sum;
+  result[40] = sum * (1.0 + 1e-5) < delta ? 0.0 : 1.0;
+  *ticket = 0;
+}
+
+// The filtering pair launch on the current outer lists, with the lists regrown
+// until the longest filtered list fits; false if skip was set (nothing ran).
+static bool refilter(System& s, bool compute, const double* skip) {
+  Grid& g = s.grid;
+  ensure_partials(s, g.nTiles);
+  for (;;) {
+    grow(g.dNb, g.caps.nb, (size_t)g.nTiles * g.cap * g.tileStride);
+    int* innerMax = g.dTileInfo + 2 * g.nTiles + 4;
+    CK(cudaMemsetAsync(innerMax, 0, sizeof(int), s.stream));
+    prof_begin(s, PK_PAIR);
+    device_pair_refilter(s, compute, skip);
+    prof_end(s, PK_PAIR);
+    CK(cudaMemcpyAsync(s.hResult, s.dResult, 4 * sizeof(double), cudaMemcpyDeviceToHost, s.stream));
+    if (skip) CK(cudaMemcpyAsync(s.hResult + 40, s.dResult + 40, 2 * sizeof(double), cudaMemcpyDeviceToHost, s.stream));
+    CK(cudaMemcpyAsync(s.hFlags, innerMax, sizeof(int), cudaMemcpyDeviceToHost, s.stream));
+    CK(cudaStreamSynchronize(s.stream));
+    if (skip && s.hResult[40] != 0.0) {
+      prof_drop_last(s);
+      return false;
+    }
+    const int mc = s.hFlags[0];
+    if (mc <= g.cap) return true;
+    if (mc > 65528) fatal("neighbor list build", "more than 65528 neighbors for one atom");
+    g.cap = std::min(65528, (mc + mc / 8 + 16 + 7) / 8 * 8);
+    skip = nullptr;   // covered: filter again with room for the longest list
+  }
+}
+
+void device_rebuild_two_level(System& s, bool compute) {
+  Grid& g = s.grid;
+  const int N = s.natoms;
+  if (s.listsOuter && *s.Lbox == s.outerL && s.outerDelta == outer_delta(s)) {
+    if (!s.packReady) device_pack(s);
+    const int blocks = std::min((N + SKIN_THREADS - 1) / SKIN_THREADS, 4 * 152);
+    ensure_partials(s, blocks);
+    prof_begin(s, PK_BUILD);
+    k_cover<<<blocks, SKIN_THREADS, 0, s.stream>>>(s.dR, g.dROuter, g.dSlotOf, g.dPos4, N, s.outerDelta, s.dR0,
+                                                   g.dPos0, (int2*)s.dPartials, s.dTicket, s.dResult);
+    CK(cudaGetLastError());
+    prof_end(s, PK_BUILD);
+    if (refilter(s, compute, s.dResult + 40)) return;
+  }
+  device_build_lists(s);
+  s.outerBuilds++;
+  refilter(s, compute, nullptr);
 }
 
 // ---------------------------------------------------------------------------------

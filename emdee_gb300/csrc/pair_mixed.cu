@@ -57,16 +57,41 @@ struct PairArgsF {
   double* partials;
   unsigned int* ticket;
   double* result;
+  // filtering launches (nb, count and cap above describe the outer lists): every
+  // entry within rc + skin (FP32 distance, FP64 test of the reference inside the
+  // band lo2In..hi2In) goes to the lists written here, in the outer lists' order
+  uint16_t* nbIn;
+  int* countIn;
+  int capIn;
+  float lo2In, hi2In;   // cell units^2
+  double thrIn;         // (rc + skin)^2 / L^2
+  const double* R;
+  double L;
+  int* innerMax;        // largest filtered list
 };
+
+// FP64 distance test of the reference (src/neighbor_lists.f90:247-250) for halo
+// index q of the tile whose layout is off/cst: its halo cell is the last one that
+// starts at or before q.
+__device__ __noinline__ bool refilter_exact(const PairArgsF& A, const int* off, const int* cst, int ai, int q) {
+  int lo = 0, hi = A.g.haloCells - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (off[mid] <= q) lo = mid;
+    else hi = mid - 1;
+  }
+  return exact_inside(A.R, A.L, ai, A.orig[cst[lo] + (q - off[lo])], A.thrIn);
+}
 
 // VAR 0: one atom type, Lennard-Jones with modifier MOD, no Coulomb term.
 // VAR 1: any types, any pair model and modifier, Coulomb term.
 // COUNT: also count the pairs within the cut-off (statistics launches only).
+// REFILTER (VAR 0, M > 5): walk the outer lists and write the filtered lists.
 // Lists are read 8 entries (16 bytes) per lane at a time, one chunk ahead of
 // use; padding entries point at a sentinel halo slot far from every atom, so
 // the inner loop needs no bounds test (except when M = 5, where the periodic
 // wrap would bring the sentinel back).
-template <bool COMPUTE, int VAR, int MOD, bool MINIMG, bool COUNT>
+template <bool COMPUTE, int VAR, int MOD, bool MINIMG, bool COUNT, bool REFILTER>
 __global__ void PAIR_BOUNDS k_pair_mixed(PairArgsF A) {
   // the flag is 0.0 or 1.0: tested on its bits (an FP64 compare in every thread of
   // every block would queue on the slow FP64 pipe)
@@ -103,6 +128,7 @@ __global__ void PAIR_BOUNDS k_pair_mixed(PairArgsF A) {
   // and the group's partial forces are summed by shuffles in a fixed order
   const int tpa = VAR == 1 ? A.tpa : 1, tpaShift = VAR == 1 ? A.tpaShift : 0, sub = threadIdx.x & (tpa - 1);
   const unsigned gmask = (0xFFFFFFFFu >> (32 - tpa)) << ((threadIdx.x & 31) & ~(tpa - 1));
+  int longestIn = 0;   // REFILTER: longest filtered list of this thread
   for (int li = threadIdx.x >> tpaShift; li < te - tb; li += blockDim.x >> tpaShift) {
     const int si = tb + li;
     const int qi = A.self[si];
@@ -112,6 +138,9 @@ __global__ void PAIR_BOUNDS k_pair_mixed(PairArgsF A) {
     const uint4* lp = reinterpret_cast<const uint4*>(A.nb) + ((size_t)t * capC * A.tileStride + li);
     const int ti = VAR == 1 ? htype[qi] : 0;
     float fx = 0.f, fy = 0.f, fz = 0.f;
+    int nIn = 0;
+    uint16_t* myIn = REFILTER ? A.nbIn + ((size_t)t * (A.capIn >> 3) * A.tileStride + li) * 8 : nullptr;
+    const int ai = REFILTER ? A.orig[si] : 0;
     uint4 cur = sub < nch ? __ldcs(lp + (size_t)sub * A.tileStride) : make_uint4(0u, 0u, 0u, 0u);
     for (int c = sub; c < nch; c += tpa) {
       const uint4 nxt = (c + tpa < nch) ? __ldcs(lp + (size_t)(c + tpa) * A.tileStride) : cur;
@@ -128,6 +157,10 @@ __global__ void PAIR_BOUNDS k_pair_mixed(PairArgsF A) {
           dz -= A.Mf * rintf(dz / A.Mf);
         }
         const float r2 = dx * dx + dy * dy + dz * dz;
+        if (REFILTER && (r2 < A.lo2In || (r2 < A.hi2In && refilter_exact(A, off, cst, ai, qj)))) {
+          if (nIn < A.capIn) myIn[(nIn >> 3) * (A.tileStride * 8) + (nIn & 7)] = (uint16_t)qj;
+          nIn++;
+        }
         if (VAR == 0) {
           // branch-free: every entry runs the same code; entries beyond the
           // cut-off (and sentinels) are zeroed by selects, so the 8 entries of
@@ -167,6 +200,11 @@ __global__ void PAIR_BOUNDS k_pair_mixed(PairArgsF A) {
       }
       cur = nxt;
     }
+    if (REFILTER) {   // sentinel padding of the last chunk, count
+      for (int k = nIn; k < A.capIn && (k & 7); k++) myIn[(k >> 3) * (A.tileStride * 8) + (k & 7)] = (uint16_t)A.haloCap;
+      A.countIn[si] = nIn;
+      longestIn = max(longestIn, nIn);
+    }
     for (int o = tpa >> 1; o > 0; o >>= 1) {
       fx += __shfl_xor_sync(gmask, fx, o);
       fy += __shfl_xor_sync(gmask, fy, o);
@@ -179,6 +217,10 @@ __global__ void PAIR_BOUNDS k_pair_mixed(PairArgsF A) {
       Fa[2] = f2d_exact(fz * A.invw);
     }
   }
+  if (REFILTER) {   // one atomic per warp
+    longestIn = __reduce_max_sync(0xffffffffu, longestIn);
+    if ((threadIdx.x & 31) == 0) atomicMax(A.innerMax, longestIn);
+  }
   // each pair is visited from both atoms: halve the sums.  Sums that are zero by
   // construction (energies without COMPUTE, Coulomb terms of VAR 0, the count
   // without COUNT) skip the reduction.
@@ -187,9 +229,9 @@ __global__ void PAIR_BOUNDS k_pair_mixed(PairArgsF A) {
   grid_reduce_ff<5, PAIR_MAX_THREADS, MASK>(v, reinterpret_cast<float2*>(A.partials), A.ticket, A.result);
 }
 
-template <bool COMPUTE, int VAR, int MOD, bool MINIMG, bool COUNT>
+template <bool COMPUTE, int VAR, int MOD, bool MINIMG, bool COUNT, bool REFILTER = false>
 static void launch(System& s, PairArgsF& A, size_t smem, int nTiles, int threads) {
-  auto kern = k_pair_mixed<COMPUTE, VAR, MOD, MINIMG, COUNT>;
+  auto kern = k_pair_mixed<COMPUTE, VAR, MOD, MINIMG, COUNT, REFILTER>;
   static size_t configured = 0;
   if (smem > configured) {
     CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -201,24 +243,23 @@ static void launch(System& s, PairArgsF& A, size_t smem, int nTiles, int threads
   kern<<<nTiles, threads, smem, s.stream>>>(A);
 }
 
-template <bool COMPUTE, bool MINIMG>
+template <bool COMPUTE, bool MINIMG, bool REFILTER = false>
 static void launch_lj(System& s, PairArgsF& A, size_t smem, int nt, int th, int mod) {
   switch (mod) {
-    case NONE: launch<COMPUTE, 0, NONE, MINIMG, false>(s, A, smem, nt, th); break;
-    case SHIFTED: launch<COMPUTE, 0, SHIFTED, MINIMG, false>(s, A, smem, nt, th); break;
-    case SHIFTED_FORCE: launch<COMPUTE, 0, SHIFTED_FORCE, MINIMG, false>(s, A, smem, nt, th); break;
-    case SMOOTHED: launch<COMPUTE, 0, SMOOTHED, MINIMG, false>(s, A, smem, nt, th); break;
-    case SHIFTED_SMOOTHED: launch<COMPUTE, 0, SHIFTED_SMOOTHED, MINIMG, false>(s, A, smem, nt, th); break;
-    case SQUARE_SMOOTHED: launch<COMPUTE, 0, SQUARE_SMOOTHED, MINIMG, false>(s, A, smem, nt, th); break;
-    default: launch<COMPUTE, 0, SHIFTED_SQUARE_SMOOTHED, MINIMG, false>(s, A, smem, nt, th); break;
+    case NONE: launch<COMPUTE, 0, NONE, MINIMG, false, REFILTER>(s, A, smem, nt, th); break;
+    case SHIFTED: launch<COMPUTE, 0, SHIFTED, MINIMG, false, REFILTER>(s, A, smem, nt, th); break;
+    case SHIFTED_FORCE: launch<COMPUTE, 0, SHIFTED_FORCE, MINIMG, false, REFILTER>(s, A, smem, nt, th); break;
+    case SMOOTHED: launch<COMPUTE, 0, SMOOTHED, MINIMG, false, REFILTER>(s, A, smem, nt, th); break;
+    case SHIFTED_SMOOTHED: launch<COMPUTE, 0, SHIFTED_SMOOTHED, MINIMG, false, REFILTER>(s, A, smem, nt, th); break;
+    case SQUARE_SMOOTHED: launch<COMPUTE, 0, SQUARE_SMOOTHED, MINIMG, false, REFILTER>(s, A, smem, nt, th); break;
+    default: launch<COMPUTE, 0, SHIFTED_SQUARE_SMOOTHED, MINIMG, false, REFILTER>(s, A, smem, nt, th); break;
   }
 }
 
-// variant: 0 single-type Lennard-Jones without charges, 1 general, 2 pair count only
-void device_pair_forces_mixed(System& s, bool compute, bool useInRc, double rc2scaled, int variant) {
+// kernel arguments and shared-memory size of a launch on the current lists
+static size_t pair_args(System& s, bool useInRc, double rc2scaled, bool general, PairArgsF& A) {
   Grid& g = s.grid;
   const double L = *s.Lbox, w = L / g.M;
-  PairArgsF A;
   A.g = make_geom(g.M, g.TB);
   A.tab = g.dHaloTab;
   A.layout = g.dLayout;
@@ -244,8 +285,25 @@ void device_pair_forces_mixed(System& s, bool compute, bool useInRc, double rc2s
   A.partials = s.dPartials;
   A.ticket = s.dTicket;
   A.result = s.dResult;
+  A.nbIn = nullptr;
+  A.countIn = nullptr;
+  A.capIn = 0;
+  A.lo2In = A.hi2In = 0.f;
+  A.thrIn = 0.0;
+  A.R = nullptr;
+  A.L = L;
+  A.innerMax = nullptr;
   size_t smem = (size_t)(g.maxHalo + 1) * sizeof(float4) + sizeof(int) * (3 * g.haloCells + 1);
-  if (variant != 0) smem += sizeof(PairEntry<float>) * s.ntypes * s.ntypes + g.maxHalo + 17;
+  if (general) smem += sizeof(PairEntry<float>) * s.ntypes * s.ntypes + g.maxHalo + 17;
+  return smem;
+}
+
+// variant: 0 single-type Lennard-Jones without charges, 1 general, 2 pair count only
+void device_pair_forces_mixed(System& s, bool compute, bool useInRc, double rc2scaled, int variant) {
+  Grid& g = s.grid;
+  const double L = *s.Lbox;
+  PairArgsF A;
+  const size_t smem = pair_args(s, useInRc, rc2scaled, variant != 0, A);
   const bool mi = g.M == 5;
   // Threads per atom: systems too small to fill the GPU with one thread per atom
   // (fewer than ~2048 threads per SM) and with long lists (more than 48 entries per
@@ -278,6 +336,37 @@ void device_pair_forces_mixed(System& s, bool compute, bool useInRc, double rc2s
   } else {
     if (mi) launch<false, 1, -1, true, true>(s, A, smem, nt, th); else launch<false, 1, -1, false, true>(s, A, smem, nt, th);
   }
+  CK(cudaGetLastError());
+}
+
+// The pair kernel over the outer lists (single-type Lennard-Jones, M > 5): forces
+// as above, and every outer entry within rc + skin written to the lists (their
+// capacity g.cap, largest list into the grid's info array).
+void device_pair_refilter(System& s, bool compute, const double* skip) {
+  Grid& g = s.grid;
+  const double L = *s.Lbox, invL2 = 1.0 / (L * L);
+  const bool useInRc = s.useInRc[s.layer - 1] != 0;
+  PairArgsF A;
+  const size_t smem = pair_args(s, false, (useInRc ? s.InRcSq : s.RcSq) * invL2, false, A);
+  A.nb = g.dNbOuter;
+  A.count = g.dNbCountOuter;
+  A.cap = g.capOuter;
+  A.skip = skip;
+  A.tpa = 1;
+  A.tpaShift = 0;
+  A.nbIn = g.dNb;
+  A.countIn = g.dNbCount;
+  A.capIn = g.cap;
+  A.thrIn = s.xRcSq * invL2;   // src/neighbor_lists.f90:213-214
+  const double M2 = (double)g.M * g.M;
+  A.lo2In = (float)(A.thrIn * M2 * (1.0 - LIST_BAND));
+  A.hi2In = (float)(A.thrIn * M2 * (1.0 + LIST_BAND));
+  A.R = s.dR;
+  A.innerMax = g.dTileInfo + 2 * g.nTiles + 4;
+  const int th = std::max(halo_min_threads(A.g), std::min(PAIR_THREADS, std::max(32, g.tileStride)));
+  const int mod = s.P(0, 0, s.layer - 1).model.p.modifier;
+  if (compute) launch_lj<true, false, true>(s, A, smem, g.nTiles, th, mod);
+  else launch_lj<false, false, true>(s, A, smem, g.nTiles, th, mod);
   CK(cudaGetLastError());
 }
 

@@ -73,7 +73,7 @@ struct Kiss {
 // ---- neighbor machinery ------------------------------------------------------
 
 struct GridCaps {   // allocated capacities of the grid arrays
-  size_t ranks = 0, atoms = 0, tiles = 0, nb = 0, scan = 0;
+  size_t ranks = 0, atoms = 0, tiles = 0, nb = 0, scan = 0, nbOuter = 0, outerAtoms = 0;
 };
 
 // Ewald k-space solver (src/kspace_ewald.f90, src/modelClass_kspace.f90):
@@ -143,6 +143,13 @@ struct Grid {
   double* dRs64 = nullptr;
   uint16_t* dNb = nullptr;
   int *dNbCount = nullptr, *dNbInner = nullptr;
+  // two-level lists: the outer lists (radius rc + skin + outer skin) of the last
+  // outer build, from which the force kernel filters the lists above at rebuilds,
+  // and the coordinates of that build
+  uint16_t* dNbOuter = nullptr;
+  int* dNbCountOuter = nullptr;
+  int capOuter = 0;
+  double* dROuter = nullptr;
   int* dTileInfo = nullptr;   // per tile: atoms, halo atoms
   int2* dHaloTab = nullptr;   // per tile and halo cell: rank, packed halo coordinates
   int* dLayout = nullptr;      // per tile: halo offsets and first slots of the last build
@@ -233,6 +240,12 @@ struct System {
   bool phaseShared = false;   // R/P aliased with another system (no deferral then)
   const double* pairSkip = nullptr;   // device rebuild flag the mixed pair kernel checks first
   double builtL = 0;           // box length at the last build
+  // two-level neighbor lists (EmDee_set_outer_skin): outerSkin < 0 not set, 0 off
+  double outerSkin = -1.0;
+  bool listsOuter = false;     // the grid holds outer lists (the last full build was an outer one)
+  double outerDelta = 0, outerL = 0;   // outer skin and box length of that build
+  long outerBuilds = 0;
+  int* hFlags = nullptr;       // pinned: [0] largest filtered list of the last filtering launch
 
   // reduction scratch
   double* dPartials = nullptr;   // per tile: Epair, Ecoul, Wpair, Wcoul, pairs within rc
@@ -271,7 +284,22 @@ void prof_drop_last(System& s);
 // the lists must be rebuilt.  Synchronizes the stream.
 bool device_skin_check(System& s);
 // Cell binning, tile sort and neighbor-list build (src/neighbor_lists.f90:63-300).
+// With two-level lists active it builds the outer lists (radius rc + skin + outer skin).
 void device_build_lists(System& s);
+// Two-level lists: the outer skin in effect for the system (0 = single-level lists),
+// and whether the next rebuild goes through them.
+double outer_delta(System& s);
+bool two_level_active(System& s);
+// A rebuild with two-level lists: if the outer lists still cover every pair within
+// rc + skin, the force kernel filters them into new lists while computing this
+// step's forces; otherwise an outer build comes first.  Leaves the forces, sums and
+// lists of a rebuild (hResult[0..3]).
+void device_rebuild_two_level(System& s, bool compute);
+// the single-type Lennard-Jones variant of the mixed-precision pair kernel applies
+bool pair_lj_only(System& s);
+// launches the mixed-precision pair kernel that also filters the outer lists into
+// the lists (skip: device flag, the launch returns at once if it is non-zero)
+void device_pair_refilter(System& s, bool compute, const double* skip);
 // Per-step position packing for the force kernels.
 void device_pack(System& s);
 // Pair forces, energies and virials of the current layer into s.F();

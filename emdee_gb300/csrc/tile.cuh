@@ -58,7 +58,24 @@ __host__ __device__ __forceinline__ int halo_rank(const TileGeom& g, int t, int 
   return cell_rank(g, wrap(tx * g.TB + hx - 2, g.M), wrap(ty * g.TB + hy - 2, g.M), wrap(tz * g.TB + hz - 2, g.M));
 }
 
+// Relative width of the band around (rc + skin)^2 inside which the list builds
+// replace the FP32 distance by the reference's FP64 test.
+constexpr double LIST_BAND = 4e-5;
+
 #ifdef __CUDACC__
+
+// FP64 minimum-image distance test of src/neighbor_lists.f90:247-250, with
+// explicitly rounded operations (the same result in every file, whatever its
+// contraction setting).
+static __device__ __noinline__ bool exact_inside(const double* R, double L, int a, int b, double thr) {
+  double r2 = 0.0;
+  for (int k = 0; k < 3; k++) {
+    const double x = __dsub_rn(__ddiv_rn(R[3 * a + k], L), __ddiv_rn(R[3 * b + k], L));
+    const double d = __dsub_rn(x, round(x));
+    r2 = __dadd_rn(r2, __dmul_rn(d, d));
+  }
+  return r2 < thr;
+}
 
 // Exclusive scan over n <= blockDim.x * ITEMS ints held in shared memory
 // (in place); returns the total.  All threads of the block must call it.

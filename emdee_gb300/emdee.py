@@ -101,6 +101,8 @@ SIGNATURES = {
     "EmDee_bond_harmonic": (_P, [_D, _D]),
     "EmDee_angle_harmonic": (_P, [_D, _D]),
     "EmDee_set_precision": (None, [tEmDee, _I]),
+    "EmDee_set_outer_skin": (None, [tEmDee, _D]),
+    "EmDee_outer_builds": (C.c_long, [tEmDee]),
     "EmDee_neighbor_pairs": (C.c_long, [tEmDee, _P, C.c_long]),
     "EmDee_destroy": (None, [_PT]),
     "EmDee_cuda_stream": (_P, [tEmDee]),
@@ -133,7 +135,7 @@ SIGNATURES = {
 }
 
 # entry points of the GB300 library with no counterpart in the reference
-EXTENSIONS = {"EmDee_set_precision", "EmDee_neighbor_pairs", "EmDee_destroy", "EmDee_cuda_stream",
+EXTENSIONS = {"EmDee_set_precision", "EmDee_set_outer_skin", "EmDee_outer_builds", "EmDee_neighbor_pairs", "EmDee_destroy", "EmDee_cuda_stream",
               "EmDee_profile", "EmDee_kernel_times", "EmDee_pair_statistics",
               "EmDee_launch_count", "EmDee_boost_noalloc", "EmDee_replicas_create", "EmDee_replicas_run",
               "EmDee_replicas_block_size", "EmDee_replicas_destroy", "EmDee_replicas_evaluate",

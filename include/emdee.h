@@ -217,6 +217,17 @@ void* EmDee_angle_harmonic(double k, double theta0);                         /* 
  * ("mixed" or "fp64") sets the default for systems created afterwards. */
 void EmDee_set_precision(tEmDee md, int mode);
 
+/* Two-level neighbor lists (mixed precision, single-type Lennard-Jones, one
+ * layer): outer lists of radius rc + skin + delta are built only when atoms have
+ * moved too far for them; at every other rebuild the force kernel filters them
+ * into the lists the reference builds (same rebuild schedule, same pair sets).
+ * delta > 0 enables them, 0 disables them, delta < 0 leaves the default (off, or
+ * the EMDEE_OUTER_SKIN environment variable).  They pay when many rebuilds fit in
+ * one outer skin (slow dynamics); on a hot fluid they do not. */
+void EmDee_set_outer_skin(tEmDee md, double delta);
+/* Number of outer builds so far (two-level lists). */
+long EmDee_outer_builds(tEmDee md);
+
 /* Writes the current neighbor pairs (1-based, i<j, sorted by i then j) to
  * pairs[2*k], pairs[2*k+1]; returns the number of pairs, or -count when
  * capacity is too small.  Used to compare pair sets with the reference. */
