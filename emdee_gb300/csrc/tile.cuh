@@ -176,31 +176,6 @@ __device__ __forceinline__ int halo_layout_saved(const TileGeom& g, int t, const
   return off[g.haloCells];
 }
 
-// Stages the halo of tile t in the tile frame, one thread per halo cell: the
-// cell-local positions of pos4 (cell units) plus the halo cell's offset from the
-// frame origin (halo cell C, C, C).  Optionally records slots and types.
-__device__ __forceinline__ void stage_frame(const TileGeom& g, const int* off, const int* cst, const int* hxyz,
-                                            const float4* pos4, float4* hpos, int* hslot, uint8_t* htype,
-                                            const uint8_t* type8) {
-  for (int h = threadIdx.x; h < g.haloCells; h += blockDim.x) {
-    const int o = off[h], n = off[h + 1] - o, b = cst[h], c = hxyz[h];
-    const float fx = (float)((c & 255) - g.C), fy = (float)(((c >> 8) & 255) - g.C), fz = (float)((c >> 16) - g.C);
-    for (int k0 = 0; k0 < n; k0 += 4) {
-      float4 p[4];
-#pragma unroll
-      for (int u = 0; u < 4; u++)
-        if (k0 + u < n) p[u] = pos4[b + k0 + u];
-#pragma unroll
-      for (int u = 0; u < 4; u++)
-        if (k0 + u < n) {
-          hpos[o + k0 + u] = make_float4(p[u].x + fx, p[u].y + fy, p[u].z + fz, p[u].w);
-          if (hslot) hslot[o + k0 + u] = b + k0 + u;
-          if (htype) htype[o + k0 + u] = type8[b + k0 + u];
-        }
-    }
-  }
-}
-
 // Stages the halo of tile t in the tile frame with one thread per halo atom (the
 // loads of a warp cover consecutive slots of cell runs, several in flight per
 // thread).  A first pass records each halo index's cell in the x word of its
