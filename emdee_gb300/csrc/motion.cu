@@ -179,9 +179,12 @@ bool device_pair_forces(System& s, bool compute, bool speculative) {
     s.pairSkip = nullptr;
   }
   prof_end(s, PK_PAIR);
-  // speculative: the skin value and rebuild flag ([8], [9]) come back with the sums
-  CK(cudaMemcpyAsync(s.hResult, s.dResult, (speculative ? 10 : 4) * sizeof(double), cudaMemcpyDeviceToHost,
-                     s.stream));
+  // Mixed precision: the last block of the pair kernel wrote the sums, and the fused
+  // step the skin value and rebuild flag ([8], [9]), straight into the pinned hResult,
+  // so one synchronisation returns all of them.  FP64 mode copies them back.
+  if (s.precision == 1)
+    CK(cudaMemcpyAsync(s.hResult, s.dResult, (speculative ? 10 : 4) * sizeof(double), cudaMemcpyDeviceToHost,
+                       s.stream));
   CK(cudaStreamSynchronize(s.stream));
   if (speculative && s.hResult[9] != 0.0) {
     prof_drop_last(s);

@@ -1019,7 +1019,7 @@ static bool refilter(System& s, bool compute, const double* skip) {
     prof_begin(s, PK_PAIR);
     device_pair_refilter(s, compute, skip);
     prof_end(s, PK_PAIR);
-    CK(cudaMemcpyAsync(s.hResult, s.dResult, 4 * sizeof(double), cudaMemcpyDeviceToHost, s.stream));
+    // the kernel's last block wrote the sums into hResult[0..4]
     if (skip) CK(cudaMemcpyAsync(s.hResult + 40, s.dResult + 40, 2 * sizeof(double), cudaMemcpyDeviceToHost, s.stream));
     CK(cudaMemcpyAsync(s.hFlags, innerMax, sizeof(int), cudaMemcpyDeviceToHost, s.stream));
     CK(cudaStreamSynchronize(s.stream));
@@ -1261,7 +1261,8 @@ __global__ void __launch_bounds__(SKIN_THREADS) k_step_fused(double* __restrict_
                                                              const int* __restrict__ slotOf,
                                                              const float4* __restrict__ pos0, float scale,
                                                              float4* __restrict__ pos4, longlong2* partial,
-                                                             unsigned int* ticket, double* result) {
+                                                             unsigned int* ticket, double* result,
+                                                             double* hostResult) {
   __shared__ MaxPrev wsum[SKIN_THREADS / 32];
   __shared__ bool last;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1325,6 +1326,8 @@ __global__ void __launch_bounds__(SKIN_THREADS) k_step_fused(double* __restrict_
     double value = maximum + 2 * sqrt(maximum * next) + next;
     result[8] = value;
     result[9] = value > skinSq ? 1.0 : 0.0;
+    hostResult[8] = value;   // pinned host memory: read after the next synchronisation
+    hostResult[9] = result[9];
     *ticket = 0;
   }
 }
@@ -1338,7 +1341,7 @@ void device_step_fused(System& s, double CP) {
   const float scale = g.M > 0 ? (float)((double)g.M / *s.Lbox) : 0.0f;
   prof_begin(s, PK_MOVE);
 #define STEP_ARGS s.dR, s.dP, s.F(), s.dInvMass, s.dR0, N, s.pendCF[0], s.pendCF[1], CP, s.skinSq, g.dSlotOf, \
-                  g.dPos0, scale, g.dPos4, (longlong2*)s.dPartials, s.dTicket, s.dResult
+                  g.dPos0, scale, g.dPos4, (longlong2*)s.dPartials, s.dTicket, s.dResult, s.hResult
 #define STEP_LAUNCH(NK, UM, PK, FM) k_step_fused<NK, UM, PK, FM><<<blocks, SKIN_THREADS, 0, s.stream>>>(STEP_ARGS)
 #define STEP_NK(UM, PK, FM)                 \
   if (s.npend == 0) STEP_LAUNCH(0, UM, PK, FM); \
@@ -1361,9 +1364,8 @@ void device_step_fused(System& s, double CP) {
   s.packReady = pack;
 }
 
-// the skin value left by the fused step
+// the skin value left by the fused step (its last block also wrote hResult[8..9])
 bool device_skin_from_step(System& s) {
-  CK(cudaMemcpyAsync(s.hResult + 8, s.dResult + 8, 2 * sizeof(double), cudaMemcpyDeviceToHost, s.stream));
   CK(cudaStreamSynchronize(s.stream));
   return s.hResult[9] != 0.0;
 }

@@ -57,6 +57,7 @@ struct PairArgsF {
   double* partials;
   unsigned int* ticket;
   double* result;
+  double* hostResult;   // pinned host copy of the sums, written by the last block
   // filtering launches (nb, count and cap above describe the outer lists): every
   // entry within rc + skin (FP32 distance, FP64 test of the reference inside the
   // band lo2In..hi2In) goes to the lists written here, in the outer lists' order
@@ -226,7 +227,8 @@ __global__ void PAIR_BOUNDS k_pair_mixed(PairArgsF A) {
   // without COUNT) skip the reduction.
   const float v[5] = {0.5f * Ep, 0.5f * Ec, 0.5f * Wp, 0.5f * Wc, 0.5f * within};
   constexpr unsigned MASK = (COMPUTE ? (VAR == 1 ? 3u : 1u) : 0u) | (VAR == 1 ? 12u : 4u) | (COUNT ? 16u : 0u);
-  grid_reduce_ff<5, PAIR_MAX_THREADS, MASK>(v, reinterpret_cast<float2*>(A.partials), A.ticket, A.result);
+  grid_reduce_ff<5, PAIR_MAX_THREADS, MASK>(v, reinterpret_cast<float2*>(A.partials), A.ticket, A.result,
+                                            A.hostResult);
 }
 
 template <bool COMPUTE, int VAR, int MOD, bool MINIMG, bool COUNT, bool REFILTER = false>
@@ -285,6 +287,7 @@ static size_t pair_args(System& s, bool useInRc, double rc2scaled, bool general,
   A.partials = s.dPartials;
   A.ticket = s.dTicket;
   A.result = s.dResult;
+  A.hostResult = s.hResult;
   A.nbIn = nullptr;
   A.countIn = nullptr;
   A.capIn = 0;

@@ -142,12 +142,13 @@ __device__ __forceinline__ void warp_sum_ff(float (&hi)[NQ], float (&lo)[NQ]) {
     }
 }
 
-// Per-thread FP32 values -> result[q] (FP64).  partials holds NQ float2 per block.
+// Per-thread FP32 values -> result[q] (FP64), also into result2 if set.  partials holds
+// NQ float2 per block.
 // The last block (ticket) sums the partials in block order; the result does not
 // depend on block scheduling.
 template <int NQ, int THREADS, unsigned MASK = ~0u>
 __device__ __forceinline__ void grid_reduce_ff(const float (&v)[NQ], float2* partials, unsigned int* ticket,
-                                               double* result) {
+                                               double* result, double* result2 = nullptr) {
   __shared__ float2 red[NQ][THREADS / 32];
   __shared__ bool last;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
@@ -210,6 +211,7 @@ __device__ __forceinline__ void grid_reduce_ff(const float (&v)[NQ], float2* par
     if ((MASK >> q) & 1u)
       for (int w = 0; w < nw; w++) ff_add(h, l, red[q][w].x, red[q][w].y);
     result[q] = (double)h + (double)l;
+    if (result2) result2[q] = (double)h + (double)l;   // e.g. pinned host memory: no copy back
   }
   if (threadIdx.x == 0) *ticket = 0;
 }
