@@ -51,14 +51,15 @@ def setup(lib, W, threads=1, precision=None):
 
 
 def vv(lib, md, W, nsteps, step0=0, per_step=None):
-    dt = W["dt"]
+    dt, half, nprop = W["dt"], 0.5 * W["dt"], W["nprop"]
+    boost, displace, ref, opts = lib.EmDee_boost, lib.EmDee_displace, C.byref(md), md.Options
     for k in range(nsteps):
-        md.Options.Compute = ((step0 + k + 1) % W["nprop"] == 0)
+        opts.Compute = ((step0 + k + 1) % nprop == 0)
         if per_step is not None:
             per_step[0](md)
-        lib.EmDee_boost(C.byref(md), 1.0, 0.0, 0.5 * dt)
-        lib.EmDee_displace(C.byref(md), 1.0, 0.0, dt)
-        lib.EmDee_boost(C.byref(md), 1.0, 0.0, 0.5 * dt)
+        boost(ref, 1.0, 0.0, half)
+        displace(ref, 1.0, 0.0, dt)
+        boost(ref, 1.0, 0.0, half)
         if per_step is not None:
             per_step[1](md)
 

@@ -890,7 +890,7 @@ static bool build_lists(System& s, bool reuse) {
     kb<<<g.nTiles, buildThreads, smem, s.stream>>>(A);
     s.prof.total++;
     CK(cudaGetLastError());
-    int mc[2] = {0, 0};   // largest list, tile-size overflow
+    int* mc = s.hFlags + 2;   // pinned: largest list, tile-size overflow
     CK(cudaMemcpyAsync(mc, A.maxCount, 2 * sizeof(int), cudaMemcpyDeviceToHost, s.stream));
     CK(cudaStreamSynchronize(s.stream));
     if (mc[1]) return false;

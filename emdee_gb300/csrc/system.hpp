@@ -245,7 +245,8 @@ struct System {
   bool listsOuter = false;     // the grid holds outer lists (the last full build was an outer one)
   double outerDelta = 0, outerL = 0;   // outer skin and box length of that build
   long outerBuilds = 0;
-  int* hFlags = nullptr;       // pinned: [0] largest filtered list of the last filtering launch
+  int* hFlags = nullptr;       // pinned: [0] largest filtered list of the last filtering launch,
+                               // [2..3] largest list and tile-size overflow of the last list build
 
   // reduction scratch
   double* dPartials = nullptr;   // per tile: Epair, Ecoul, Wpair, Wcoul, pairs within rc
