@@ -61,20 +61,25 @@ static int motion_blocks(int N) {
 }
 
 // 2KE per dimension = sum over atoms of P^2/m (src/EmDeeData.f90:157-189, free
-// atoms), into result[10..12]
+// atoms), into result[10..12] (and the pinned host copy).  The threads walk the
+// flat array P[3N] with a grid stride that is a multiple of 3 (coalesced loads),
+// so each thread sums one component; a few hundred blocks keep the FP64 shuffle
+// reductions and the block partials few.
 template <bool UNITM>
 __global__ void __launch_bounds__(MOTION_THREADS) k_kinetic(const double* __restrict__ P,
                                                             const double* __restrict__ invMass, int N,
-                                                            double* partials, unsigned int* ticket, double* result) {
-  double k2[3] = {0.0, 0.0, 0.0};
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
-    const double im = UNITM ? 1.0 : invMass[i];
-    for (int d = 0; d < 3; d++) {
-      const double p = P[3 * i + d];
-      k2[d] += UNITM ? p * p : im * (p * p);
-    }
+                                                            double* partials, unsigned int* ticket, double* result,
+                                                            double* hostResult) {
+  const size_t n3 = 3 * (size_t)N, stride = (size_t)gridDim.x * blockDim.x;
+  const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double k = 0.0;
+  for (size_t j = g; j < n3; j += stride) {
+    const double p = P[j];
+    k += UNITM ? p * p : invMass[j / 3] * (p * p);
   }
-  grid_reduce<3, MOTION_THREADS>(k2, partials, ticket, result + 10);
+  const int d = (int)(g % 3);
+  double k2[3] = {d == 0 ? k : 0.0, d == 1 ? k : 0.0, d == 2 ? k : 0.0};
+  grid_reduce<3, MOTION_THREADS>(k2, partials, ticket, result + 10, hostResult + 10);
 }
 
 template <bool FMA>
@@ -126,16 +131,18 @@ void device_move(System& s, double CR, double CP) {
 }
 
 void device_kinetic(System& s, double* twoKE) {
-  int N = s.natoms, blocks = motion_blocks(N);
+  const int N = s.natoms;
+  // a multiple of 3 blocks (the grid stride over P[3N] must be), at most 3 per SM
+  const int blocks = std::min(3 * ((N + 3 * MOTION_THREADS - 1) / (3 * MOTION_THREADS)), 3 * 152);
   if (s.keCap < blocks) {
     CK(cudaFree(s.dKE));
     s.keCap = blocks;
     CK(cudaMalloc(&s.dKE, sizeof(double) * 3 * blocks));
   }
   auto kern = s.unitMass ? k_kinetic<true> : k_kinetic<false>;
-  kern<<<blocks, MOTION_THREADS, 0, s.stream>>>(s.dP, s.dInvMass, N, s.dKE, s.dTicket + 1, s.dResult);
+  // the last block writes the sums into the pinned hResult as well: no copy back
+  kern<<<blocks, MOTION_THREADS, 0, s.stream>>>(s.dP, s.dInvMass, N, s.dKE, s.dTicket + 1, s.dResult, s.hResult);
   CK(cudaGetLastError());
-  CK(cudaMemcpyAsync(s.hResult + 10, s.dResult + 10, 3 * sizeof(double), cudaMemcpyDeviceToHost, s.stream));
   CK(cudaStreamSynchronize(s.stream));
   for (int d = 0; d < 3; d++) twoKE[d] = s.hResult[10 + d];
 }

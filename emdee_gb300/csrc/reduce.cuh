@@ -11,7 +11,7 @@ namespace emdee {
 // Variant whose inputs are already warp sums held by lane 0 of each warp.
 template <int NQ, int THREADS>
 __device__ __forceinline__ void grid_reduce_lane0(const double (&v)[NQ], double* partials, unsigned int* ticket,
-                                                  double* result) {
+                                                  double* result, double* result2 = nullptr) {
   __shared__ double red[NQ][THREADS / 32];
   __shared__ bool last;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
@@ -63,18 +63,20 @@ __device__ __forceinline__ void grid_reduce_lane0(const double (&v)[NQ], double*
     double x = 0.0;
     for (int w = 0; w < nw; w++) x += red[threadIdx.x][w];
     result[threadIdx.x] = x;
+    if (result2) result2[threadIdx.x] = x;   // e.g. pinned host memory: no copy back
   }
   if (threadIdx.x == 0) *ticket = 0;
 }
 
 // FP64 per-thread values: warp shuffle sums, then as above.
 template <int NQ, int THREADS>
-__device__ __forceinline__ void grid_reduce(double (&v)[NQ], double* partials, unsigned int* ticket, double* result) {
+__device__ __forceinline__ void grid_reduce(double (&v)[NQ], double* partials, unsigned int* ticket, double* result,
+                                            double* result2 = nullptr) {
 #pragma unroll
   for (int q = 0; q < NQ; q++)
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_down_sync(0xffffffffu, v[q], o);
-  grid_reduce_lane0<NQ, THREADS>(v, partials, ticket, result);
+  grid_reduce_lane0<NQ, THREADS>(v, partials, ticket, result, result2);
 }
 
 // Warp sums of FP32 values with an error-free two-sum at every level; lane 0
