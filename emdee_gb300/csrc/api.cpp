@@ -834,6 +834,22 @@ void EmDee_add_dihedral(tEmDee md, int i, int j, int k, int l, void* model) {
   EmDee_ignore_pair(md, k, l);
 }
 
+// The device-side address of a caller buffer in page-locked host memory (registered
+// or allocated through CUDA), or null: kernels then read or write the caller's
+// array directly over the host link instead of a copy plus a kernel pass.
+static double* pinned_device_pointer(double* address) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, address) != cudaSuccess) {
+    cudaGetLastError();   // not a CUDA-known pointer: clear the error
+    return nullptr;
+  }
+  return at.type == cudaMemoryTypeHost ? (double*)at.devicePointer : nullptr;
+}
+
+static bool mirrors_active(const System& s) {
+  return s.hMirrorR || s.hMirrorP || s.hMirrorF || s.hMirrorLayerF;
+}
+
 // src/EmDeeCode.f90:805-925
 void EmDee_upload(tEmDee* md, char* option, double* address) {
   System& s = *sys_of(*md);
@@ -864,11 +880,14 @@ void EmDee_upload(tEmDee* md, char* option, double* address) {
     }
   } else if (!strcmp(item, "momenta")) {
     if (!s.initialized) fatal("upload", "box and coordinates have not been defined");
-    CK(cudaMemcpyAsync(s.dP, address, sizeof(double) * n3, cudaMemcpyHostToDevice, s.stream));
+    // every atom free and a pinned caller buffer: one kernel reads it, stores P and
+    // sums the kinetic energy; otherwise a copy, then the sum
+    const double* src = s.nbodies == 0 ? pinned_device_pointer(address) : nullptr;
+    if (!src) CK(cudaMemcpyAsync(s.dP, address, sizeof(double) * n3, cudaMemcpyHostToDevice, s.stream));
     if (s.hMirrorP) memcpy(s.hMirrorP, address, sizeof(double) * n3);
     double t2[3] = {0, 0, 0}, r2[3] = {0, 0, 0};   // src/EmDeeData.f90:157-189
     if (s.nbodies == 0) {
-      device_kinetic(s, t2);   // every atom is free: sum on the device
+      device_kinetic(s, t2, src);   // every atom is free: sum on the device
     } else {
       for (int i : s.freeList)
         for (int d = 0; d < 3; d++) t2[d] += s.invMass[i] * (address[3 * i + d] * address[3 * i + d]);
@@ -911,10 +930,18 @@ void EmDee_upload(tEmDee* md, char* option, double* address) {
 
 // src/EmDeeCode.f90:659-801 (free-atom options)
 void EmDee_download(tEmDee md, char* option, double* address) {
-  flush_pending(*sys_of(md));
   System& s = *sys_of(md);
   char item[257];
   option_string(option, item);
+  // Pending kicks change only P: the coordinates and the box leave them pending, and a
+  // momenta download of free atoms into a pinned buffer applies them in its own pass
+  // (k_kick_out).  Everything else, and every download while host mirrors are in use,
+  // applies them first.
+  const bool isR = !strcmp(item, "coordinates") || !strcmp(item, "box");
+  double* kickOut = nullptr;
+  if (!strcmp(item, "momenta") && s.npend > 0 && s.nbodies == 0 && !mirrors_active(s) && address)
+    kickOut = pinned_device_pointer(address);
+  if (mirrors_active(s) || !(isR || kickOut)) flush_pending(s);
   if (!address) fatal("download", "provided address is invalid");
   size_t b = sizeof(double) * 3 * s.natoms;
   MirrorScope scope(s);
@@ -924,7 +951,9 @@ void EmDee_download(tEmDee md, char* option, double* address) {
     if (!s.hasR) fatal("download", "coordinates have not been allocated");
     CK(cudaMemcpyAsync(address, s.dR, b, cudaMemcpyDeviceToHost, s.stream));
   } else if (!strcmp(item, "momenta")) {
-    if (s.nbodies == 0) {
+    if (kickOut) {
+      device_kick_out(s, kickOut);
+    } else if (s.nbodies == 0) {
       CK(cudaMemcpyAsync(address, s.dP, b, cudaMemcpyDeviceToHost, s.stream));
     } else {   // free atoms: P; body atoms: particle momenta (src/EmDeeCode.f90:729-741)
       double* tmp;

@@ -65,8 +65,10 @@ static int motion_blocks(int N) {
 // flat array P[3N] with a grid stride that is a multiple of 3 (coalesced loads),
 // so each thread sums one component; a few hundred blocks keep the FP64 shuffle
 // reductions and the block partials few.
-template <bool UNITM>
-__global__ void __launch_bounds__(MOTION_THREADS) k_kinetic(const double* __restrict__ P,
+// COPY: the momenta come from src (the caller's pinned host buffer, read over the
+// host link) and are stored into P on the way.
+template <bool UNITM, bool COPY>
+__global__ void __launch_bounds__(MOTION_THREADS) k_kinetic(const double* __restrict__ src, double* __restrict__ P,
                                                             const double* __restrict__ invMass, int N,
                                                             double* partials, unsigned int* ticket, double* result,
                                                             double* hostResult) {
@@ -74,7 +76,8 @@ __global__ void __launch_bounds__(MOTION_THREADS) k_kinetic(const double* __rest
   const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   double k = 0.0;
   for (size_t j = g; j < n3; j += stride) {
-    const double p = P[j];
+    const double p = src[j];
+    if (COPY) P[j] = p;
     k += UNITM ? p * p : invMass[j / 3] * (p * p);
   }
   const int d = (int)(g % 3);
@@ -130,7 +133,43 @@ void device_move(System& s, double CR, double CP) {
   else move_launch<false>(s, CR, CP);
 }
 
-void device_kinetic(System& s, double* twoKE) {
+// Pending kicks applied on the way out (free atoms, CP = 1): P += CF_k F for each
+// pending k in order, with the arithmetic of k_boost, into P and straight into the
+// caller's pinned host buffer out.
+template <int NK, bool FMA>
+__global__ void __launch_bounds__(MOTION_THREADS) k_kick_out(double* __restrict__ P, const double* __restrict__ F,
+                                                             size_t n3, double cf0, double cf1,
+                                                             double* __restrict__ out) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x; j < n3; j += stride) {
+    const double f = F[j];
+    double p = P[j];
+    p = FMA ? fma(cf0, f, p) : p + cf0 * f;
+    if (NK == 2) p = FMA ? fma(cf1, f, p) : p + cf1 * f;
+    P[j] = p;
+    out[j] = p;
+  }
+}
+
+void device_kick_out(System& s, double* out) {
+  const size_t n3 = 3 * (size_t)s.natoms;
+  const int blocks = (int)std::min<size_t>((n3 + MOTION_THREADS - 1) / MOTION_THREADS, 8 * 152);
+  const double c0 = s.pendCF[0], c1 = s.pendCF[1];
+  prof_begin(s, PK_BOOST);
+  if (s.precision == 0) {
+    if (s.npend == 1) k_kick_out<1, true><<<blocks, MOTION_THREADS, 0, s.stream>>>(s.dP, s.F(), n3, c0, c1, out);
+    else k_kick_out<2, true><<<blocks, MOTION_THREADS, 0, s.stream>>>(s.dP, s.F(), n3, c0, c1, out);
+  } else {
+    if (s.npend == 1) k_kick_out<1, false><<<blocks, MOTION_THREADS, 0, s.stream>>>(s.dP, s.F(), n3, c0, c1, out);
+    else k_kick_out<2, false><<<blocks, MOTION_THREADS, 0, s.stream>>>(s.dP, s.F(), n3, c0, c1, out);
+  }
+  CK(cudaGetLastError());
+  prof_end(s, PK_BOOST);
+  s.npend = 0;
+  CK(cudaStreamSynchronize(s.stream));
+}
+
+void device_kinetic(System& s, double* twoKE, const double* src) {
   const int N = s.natoms;
   // a multiple of 3 blocks (the grid stride over P[3N] must be), at most 3 per SM
   const int blocks = std::min(3 * ((N + 3 * MOTION_THREADS - 1) / (3 * MOTION_THREADS)), 3 * 152);
@@ -139,9 +178,11 @@ void device_kinetic(System& s, double* twoKE) {
     s.keCap = blocks;
     CK(cudaMalloc(&s.dKE, sizeof(double) * 3 * blocks));
   }
-  auto kern = s.unitMass ? k_kinetic<true> : k_kinetic<false>;
+  auto kern = src ? (s.unitMass ? k_kinetic<true, true> : k_kinetic<false, true>)
+                 : (s.unitMass ? k_kinetic<true, false> : k_kinetic<false, false>);
   // the last block writes the sums into the pinned hResult as well: no copy back
-  kern<<<blocks, MOTION_THREADS, 0, s.stream>>>(s.dP, s.dInvMass, N, s.dKE, s.dTicket + 1, s.dResult, s.hResult);
+  kern<<<blocks, MOTION_THREADS, 0, s.stream>>>(src ? src : s.dP, s.dP, s.dInvMass, N, s.dKE, s.dTicket + 1,
+                                                s.dResult, s.hResult);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(s.stream));
   for (int d = 0; d < 3; d++) twoKE[d] = s.hResult[10 + d];

@@ -311,7 +311,13 @@ void device_pack(System& s);
 bool device_pair_forces(System& s, bool compute, bool speculative = false);
 // P <- CP P + CF F (free atoms); optional 2KE per dimension into hResult[10..12].
 void device_boost(System& s, double CP, double CF, bool kinetic);
-void device_kinetic(System& s, double* twoKE);   // free atoms only (no bodies)
+// 2KE per dimension of the momenta, free atoms only (no bodies); src: the momenta are
+// read from there (a device-accessible pointer to the caller's pinned buffer) and
+// stored into P on the way
+void device_kinetic(System& s, double* twoKE, const double* src = nullptr);
+// applies the pending kicks (1 or 2) and writes the momenta to P and to out (a
+// device-accessible pointer to the caller's pinned buffer); synchronizes
+void device_kick_out(System& s, double* out);
 // bonds and angles of the current layer: adds their forces to F and returns
 // Ebond, Wbond, Eangle, Wangle and the Coulomb discount energy; false if none ran
 bool device_bonded(System& s, double out[5]);
