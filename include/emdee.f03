@@ -250,6 +250,17 @@ interface
     integer(c_int), value :: mode
   end subroutine EmDee_set_precision
 
+  subroutine EmDee_set_outer_skin( md, delta ) bind(C,name="EmDee_set_outer_skin")
+    import
+    type(tEmDee), value :: md
+    real(c_double), value :: delta
+  end subroutine EmDee_set_outer_skin
+
+  integer(c_long) function EmDee_outer_builds( md ) bind(C,name="EmDee_outer_builds")
+    import
+    type(tEmDee), value :: md
+  end function EmDee_outer_builds
+
   subroutine EmDee_destroy( md ) bind(C,name="EmDee_destroy")
     import
     type(tEmDee), intent(inout) :: md
