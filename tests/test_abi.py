@@ -61,3 +61,17 @@ def test_oracle_exports_same_abi(oracle_path):
     exported = set(re.findall(r"\bT (EmDee_\w+)", out))
     assert set(declared_symbols()) - EXTENSIONS - {"EmDee_set_precision", "EmDee_neighbor_pairs",
                                                    "EmDee_destroy"} <= exported
+
+
+def test_fortran_module_matches_c_header():
+    """include/emdee.f03 binds every reference entry point of include/emdee.h (the
+    C-only extensions for batches, the surrogate and profiling aside), and nothing
+    the C header does not declare."""
+    f03 = open(os.path.join(ROOT, "include", "emdee.f03")).read()
+    bound = set(re.findall(r'bind\(C,\s*name="(EmDee_\w+)"\)', f03))
+    c_only = {"EmDee_boost_noalloc", "EmDee_cuda_stream", "EmDee_device_pointer", "EmDee_kernel_times",
+              "EmDee_launch_count", "EmDee_neighbor_pairs", "EmDee_pair_statistics", "EmDee_profile"}
+    c_only |= {n for n in EXTENSIONS if n.startswith(("EmDee_replicas_", "EmDee_surrogate_"))}
+    declared = set(declared_symbols())
+    assert bound <= declared, sorted(bound - declared)
+    assert declared - c_only <= bound, sorted(declared - c_only - bound)
