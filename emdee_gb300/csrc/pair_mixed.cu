@@ -26,8 +26,8 @@ static const int PAIR_THREADS = 256;   // upper bound; launches use one thread p
 static const int PAIR_THREADS_GENERAL = 1024;
 #define PAIR_MAX_THREADS (VAR == 1 ? PAIR_THREADS_GENERAL : PAIR_THREADS)
 // PAIR_MIN_BLOCKS (compile-time): resident blocks per SM the register budget must allow
-#ifdef PAIR_MIN_BLOCKS
-#define PAIR_BOUNDS __launch_bounds__(PAIR_MAX_THREADS, PAIR_MIN_BLOCKS)
+#ifdef PAIR_MIN_BLOCKS   // single-type Lennard-Jones variant only
+#define PAIR_BOUNDS __launch_bounds__(PAIR_MAX_THREADS, (VAR == 0 && !REFILTER) ? PAIR_MIN_BLOCKS : 1)
 #else
 #define PAIR_BOUNDS __launch_bounds__(PAIR_MAX_THREADS)
 #endif
