@@ -6,9 +6,11 @@ lattice jittered by U(+-0.05 sigma) (seed 86245), reduced density 0.8442
 (L = 107.494), lj_cut with rc = 2.5, neighbor skin 0.3, Maxwell-Boltzmann
 momenta at T* = 1.5 from EmDee_random_momenta, dt = 0.005.  One step is the
 reference's velocity-Verlet loop body (test/common/contained.f90:63-72):
-EmDee_boost(dt/2), EmDee_displace(dt), EmDee_boost(dt/2), energies every 100
-steps, neighbor lists rebuilt whenever the skin check fires.  FP32 pair math,
-FP64 positions, momenta, energy and virial sums.
+EmDee_boost(dt/2), EmDee_displace(dt), EmDee_boost(dt/2), with the potential
+energy and virial of every step (Options%Compute at every step: the workload's
+outputs are per-step forces, energy and virial), neighbor lists rebuilt
+whenever the skin check fires.  FP32 pair math, FP64 positions, momenta,
+energy and virial sums.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -31,7 +33,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WORKLOAD = dict(name="lj_fcc_1048576", N=4 * 64 ** 3, rho=0.8442, rc=2.5, skin=0.3, kT=1.5, dt=0.005,
-                seed=86245, jitter=0.05, nprop=100)
+                seed=86245, jitter=0.05, nprop=1)
 METRIC = "atom-steps/s"
 ORACLE_SO = os.path.join(ROOT, "oracle", "_build", "liboracle_emdee.so")
 
@@ -48,6 +50,15 @@ def setup(lib, W, threads=1, precision=None):
     lib.upload(md, "coordinates", R)
     lib.EmDee_random_momenta(C.byref(md), W["kT"], True, W["seed"])
     return md
+
+
+def workload_config(W, world=1):
+    """The config dict both arms print (same workload, same keys)."""
+    cfg = {"workload": W["name"], "N": W["N"], "rho": W["rho"], "L": (W["N"] / W["rho"]) ** (1 / 3),
+           "rc": W["rc"], "skin": W["skin"], "kT": W["kT"], "dt": W["dt"], "energies_every": W["nprop"],
+           "parallelism": "replicas" if world > 1 else "single GPU",
+           "l2": "no flush; per-step working set (R, P, F, packed positions, lists) ~0.4 GB > 129 MB L2"}
+    return cfg
 
 
 def vv(lib, md, W, nsteps, step0=0, per_step=None):
@@ -185,8 +196,7 @@ def run_reference(args):
             "steps": n, "warmup": args.warmup, "ms_per_step": 1e3 * t / max(n, 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded fcc lattice)",
-            "config": {"workload": W["name"], "N": W["N"], "rho": W["rho"], "rc": W["rc"], "skin": W["skin"],
-                       "dt": W["dt"]},
+            "config": workload_config(W, world=int(os.environ.get("WORLD_SIZE", "1"))),
             "cpu_baseline": {"value": rate, "unit": "atom-steps/s", "cores": threads, "kind": "port",
                              "sample": "%d velocity-Verlet steps of the full %d-atom box (%.1f s, capped at 150 s)"
                                        % (n, W["N"], t)},
@@ -197,6 +207,26 @@ def run_reference(args):
 # ---------------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------------
+
+def link_rates(torch, nbytes, reps=10):
+    """Host link rates for reference: one cudaMemcpyAsync of nbytes each way between
+    pinned host memory and the device (torch copy_, best of reps, CUDA events)."""
+    h = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    out = {"bytes": nbytes}
+    for name, dst, src in (("h2d_gbs", d, h), ("d2h_gbs", h, d)):
+        best = 0.0
+        for _ in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            dst.copy_(src, non_blocking=True)
+            b.record()
+            b.synchronize()
+            best = max(best, nbytes / (a.elapsed_time(b) * 1e-3) / 1e9)
+        out[name] = best
+    del h, d
+    return out
+
 
 def max_over_ranks(x, world, device):
     """The largest value of x over the ranks of the job (x itself for one rank): the
@@ -327,9 +357,10 @@ def run_gpu(args):
     barrier()
     e2e_rate, e2e_ms = job_rate(N * ne2e, f0.elapsed_time(f1), world, "cuda")
     e2e = {"value": e2e_rate, "unit": "atom-steps/s", "h2d_bytes_per_step": 24 * N,
-           "d2h_bytes_per_step": 48 * N + 40, "steps": ne2e,
+           "d2h_bytes_per_step": 48 * N + 40, "steps": ne2e, "ms_per_step": e2e_ms / ne2e,
            "per_step": "EmDee_upload(momenta) from pinned host memory, boost/displace/boost, "
-                       "EmDee_download(coordinates) and EmDee_download(momenta) into pinned host memory"}
+                       "EmDee_download(coordinates) and EmDee_download(momenta) into pinned host memory",
+           "link": link_rates(torch, 50 * 2 ** 20)}
 
     # ---- the other workloads: replica batch and rigid water (throughput only) ----
     extra = {}
@@ -351,12 +382,7 @@ def run_gpu(args):
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32 pair math, f64 state",
                 "data": "synthetic (seeded fcc lattice, Maxwell-Boltzmann momenta)",
-                "config": {"workload": W["name"], "N": N, "rho": W["rho"], "L": (N / W["rho"]) ** (1 / 3),
-                           "rc": W["rc"], "skin": W["skin"], "kT": W["kT"], "dt": W["dt"],
-                           "energies_every": W["nprop"], "neighbor_builds_in_timed_region": builds,
-                           "parallelism": "replicas" if world > 1 else "single GPU",
-                           "l2": "no flush; per-step working set (R, P, F, packed positions, lists) ~0.4 GB "
-                                 "> 129 MB L2"},
+                "config": workload_config(W, world=world), "neighbor_builds_in_timed_region": builds,
                 "clocks": clk, "gpu_launches": int(launches), "roofline": roofline, "roofline_hbm": roofline_hbm,
                 "roofline_step": roofline_step,
                 "kernels": per_kernel, "e2e": e2e, "cpu_baseline": cpu, "workloads": extra}
@@ -426,8 +452,32 @@ def measure_water(lib, pkg, torch, steps):
     out = {"metric": METRIC, "value": 12288 * steps / (ms * 1e-3), "unit": "atom-steps/s", "atoms": 12288,
            "steps": steps, "ms_per_step": ms / steps,
            "timing": "CUDA events on the library stream around the velocity-Verlet loop",
-           "errors_vs_fp64_oracle": "tests/test_gpu_water_box.py (forces 1.6e-5 relative RMS, energies <= 4e-5)"}
+           "errors_vs_fp64": water_errors(lib, pkg, md)}
     lib.lib.EmDee_destroy(C.byref(md))
+    return out
+
+
+def water_errors(lib, pkg, md):
+    """Errors of the mixed-precision results at the run's final configuration against
+    FP64 arithmetic on the same coordinates: a second system in the library's FP64
+    mode, whose forces, energies and virial match the FP64 oracle to 1e-12
+    (tests/test_gpu_water_box.py, tests/test_gpu_models.py)."""
+    N = 12288
+    R = lib.download(md, "coordinates", (N, 3))
+    md.Options.Compute = True
+    lib.EmDee_compute_forces(C.byref(md))
+    F32 = lib.download(md, "forces", (N, 3))
+    ref = setup_water_box(lib, 4096, 86245, precision=pkg.FP64)
+    lib.upload(ref, "coordinates", R)
+    ref.Options.Compute = True
+    lib.EmDee_compute_forces(C.byref(ref))
+    F64 = lib.download(ref, "forces", (N, 3))
+    out = {"force_rel_rms": float(np.sqrt(((F32 - F64) ** 2).sum() / (F64 ** 2).sum())),
+           "potential_rel": abs(md.Energy.Potential / ref.Energy.Potential - 1),
+           "coulomb_rel": abs(md.Energy.Coulomb / ref.Energy.Coulomb - 1),
+           "virial_rel": abs(md.Virial.Total / ref.Virial.Total - 1),
+           "reference": "library FP64 mode at the final configuration of the run"}
+    lib.lib.EmDee_destroy(C.byref(ref))
     return out
 
 
@@ -490,7 +540,7 @@ def main():
     ap.add_argument("--no-hmc", action="store_true", help="skip the surrogate-HMC measurement")
     ap.add_argument("--hmc-iterations", type=int, default=50)
     ap.add_argument("--hmc-configs", type=int, default=20000)
-    ap.add_argument("--water-steps", type=int, default=300)
+    ap.add_argument("--water-steps", type=int, default=500)
     ap.add_argument("--atoms", type=int, default=None,
                     help="smaller box of the same density (profiling runs); default 1,048,576")
     args = ap.parse_args()

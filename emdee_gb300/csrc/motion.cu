@@ -27,7 +27,7 @@ template <bool KIN, bool UNITCP, bool UNITM, bool FMA>
 __global__ void __launch_bounds__(MOTION_THREADS) k_boost(double* __restrict__ P, const double* __restrict__ F,
                                                           const double* __restrict__ invMass, int N, double CP,
                                                           double CF, double* partials, unsigned int* ticket,
-                                                          double* result) {
+                                                          double* twoKE) {
   double k2[3] = {0.0, 0.0, 0.0};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
     double im = (KIN && !UNITM) ? invMass[i] : 1.0;
@@ -38,7 +38,7 @@ __global__ void __launch_bounds__(MOTION_THREADS) k_boost(double* __restrict__ P
       if (KIN) k2[d] += UNITM ? p * p : im * (p * p);
     }
   }
-  if (KIN) grid_reduce<3, MOTION_THREADS>(k2, partials, ticket, result + 10);
+  if (KIN) grid_reduce<3, MOTION_THREADS>(k2, partials, ticket, twoKE);
 }
 
 template <bool UNITCR, bool UNITM, bool FMA>
@@ -55,9 +55,12 @@ __global__ void __launch_bounds__(MOTION_THREADS) k_move(double* __restrict__ R,
   }
 }
 
+// grid size cap of the boost kernels: 152 SMs x 8 resident blocks, grid-stride beyond
+static constexpr int MOTION_MAX_BLOCKS = 1184;
+
 static int motion_blocks(int N) {
   int b = (N + MOTION_THREADS - 1) / MOTION_THREADS;
-  return b < 1184 ? b : 1184;   // 152 SMs x 8 resident blocks, grid-stride beyond
+  return b < MOTION_MAX_BLOCKS ? b : MOTION_MAX_BLOCKS;
 }
 
 // 2KE per dimension = sum over atoms of P^2/m (src/EmDeeData.f90:157-189, free
@@ -98,7 +101,7 @@ static void boost_launch(System& s, double CP, double CF, bool kinetic) {
     auto kern = CP == 1.0 ? (s.unitMass ? k_boost<true, true, true, FMA> : k_boost<true, true, false, FMA>)
                           : (s.unitMass ? k_boost<true, false, true, FMA> : k_boost<true, false, false, FMA>);
     kern<<<blocks, MOTION_THREADS, 0, s.stream>>>(s.dP, s.F(), s.dInvMass, N, CP, CF, s.dKE, s.dTicket + 1,
-                                                  s.dResult);
+                                                  s.dResult + 10);
     CK(cudaGetLastError());
     prof_end(s, PK_BOOST);
     CK(cudaMemcpyAsync(s.hResult + 10, s.dResult + 10, 3 * sizeof(double), cudaMemcpyDeviceToHost, s.stream));
@@ -270,11 +273,12 @@ void device_pair_statistics(System& s, long* listed, long* within) {
 // EmDee_boost_noalloc: the boost + kinetic-energy kernel on caller-owned device
 // arrays, with its scratch in a fixed device array instead of cudaMalloc.
 //
-// Who needs it: callers that must not allocate device memory at this point,
-// such as code running in a cudaLaunchHostFunc callback (CUDA calls that
-// allocate are not permitted there), loops that cannot afford the device-wide
-// synchronization that cudaMalloc/cudaFree may imply, and processes whose
-// device memory is entirely reserved by another allocator.
+// Who needs it: callers that must not allocate device memory at the point of
+// the call -- processes whose device memory is owned by another allocator (a
+// framework's caching allocator or a pool reserved at start-up), and loops that
+// cannot take the device-wide synchronization that cudaMalloc/cudaFree may
+// imply.  It is called from ordinary host code, like every entry point: CUDA
+// forbids CUDA calls inside a stream's host function, and this one makes some.
 //
 // The scratch holds one partial sum per thread block (3 doubles) and the
 // completion ticket of the grid reduction.  It lives in every GPU that loads
@@ -287,7 +291,8 @@ void device_pair_statistics(System& s, long* listed, long* within) {
 
 namespace {
 
-const int NOALLOC_MAX_BLOCKS = 1184;   // the grid size cap of device_boost
+const int NOALLOC_MAX_BLOCKS = MOTION_MAX_BLOCKS;   // one partial per block of the boost grid
+static_assert(NOALLOC_MAX_BLOCKS >= MOTION_MAX_BLOCKS, "the scratch must hold a partial for every block");
 const long long NOALLOC_MAX_ATOMS = 715827882LL;   // 3N must fit in a signed 32-bit index
 // [0, 3*MAX_BLOCKS) per-block partial sums; [3*MAX_BLOCKS] ticket (as 8 bytes)
 static __device__ __align__(256) double g_noalloc_scratch[3 * NOALLOC_MAX_BLOCKS + 1];
@@ -316,14 +321,19 @@ void* noalloc_scratch_address() {
 // P <- CP P + CF F for N atoms (device arrays double[N][3]) and, in twoKE
 // (device double[3]), 2KE per dimension = sum over atoms of P^2/m with the
 // updated momenta.  invMass is a device double[N] array, or NULL for unit
-// masses.  Returns 0 on success, 1 for a size outside [1, 715827882] atoms,
-// 2 for a CUDA error; the reason is printed on stderr.  Allocates no memory.
+// masses.  Returns 0 on success, 1 for a size outside [1, 715827882] atoms or a
+// NULL P, F or twoKE, 2 for a CUDA error; the reason is printed on stderr.
+// Allocates no memory.
 extern "C" int EmDee_boost_noalloc(double* P, const double* F, const double* invMass, int N, double CP, double CF,
                                    double* twoKE, void* stream) {
   using namespace emdee;
   if (N < 1 || (long long)N > NOALLOC_MAX_ATOMS) {
     fprintf(stderr, "Error in boost_noalloc: %d atoms is outside the supported range [1, %lld].\n", N,
             NOALLOC_MAX_ATOMS);
+    return 1;
+  }
+  if (!P || !F || !twoKE) {
+    fprintf(stderr, "Error in boost_noalloc: the momenta, forces and kinetic-energy arrays must not be NULL.\n");
     return 1;
   }
   double* scratch = (double*)noalloc_scratch_address();
@@ -337,7 +347,7 @@ extern "C" int EmDee_boost_noalloc(double* P, const double* F, const double* inv
   auto kern = unitCP ? (unitM ? k_boost<true, true, true, false> : k_boost<true, true, false, false>)
                      : (unitM ? k_boost<true, false, true, false> : k_boost<true, false, false, false>);
   if (e == cudaSuccess) {
-    kern<<<blocks, MOTION_THREADS, 0, st>>>(P, F, invMass, N, CP, CF, scratch, ticket, twoKE - 10);
+    kern<<<blocks, MOTION_THREADS, 0, st>>>(P, F, invMass, N, CP, CF, scratch, ticket, twoKE);
     e = cudaGetLastError();
   }
   if (e != cudaSuccess) {

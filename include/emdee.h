@@ -105,8 +105,10 @@ EMDEE_STATIC_ASSERT(sizeof(tEmDee) == 240, "tEmDee size");
 tEmDee EmDee_system(int threads, int layers, double rc, double skin, int N,
                     int* types, double* masses, int* bodies);
 
-/* src/EmDeeCode.f90:212-235 (EmDee_memory_address).  Returns a host mirror;
- * see EmDee_memory_address notes in INTEGRATION.md for the sync points. */
+/* src/EmDeeCode.f90:212-235 (EmDee_memory_address).  Returns a page-locked host
+ * mirror of the device array: the library copies it to the device when a call
+ * on this system starts and back when the call ends, so reads and writes
+ * between calls act on the system's state as with the reference's pointers. */
 void* EmDee_memory_address(tEmDee md, char* option);
 
 /* src/EmDeeCode.f90:239-269 (EmDee_share_phase_space) */
@@ -255,17 +257,18 @@ long EmDee_launch_count(tEmDee md);
 
 /* No counterpart in the reference.  EmDee_boost's momentum update and
  * kinetic-energy sums on caller-owned device arrays, allocating nothing: for
- * callers that cannot call cudaMalloc at that point (inside a
- * cudaLaunchHostFunc callback, in loops that cannot afford the synchronization
- * cudaMalloc/cudaFree may imply, or when another allocator owns the device
- * memory).  P (double[N][3], updated in place), F (double[N][3]), invMass
- * (double[N], or NULL for unit masses) and twoKE (double[3]: 2KE per
- * dimension) are device pointers; stream is a cudaStream_t (NULL: default).
- * The reduction scratch is a fixed 28 KB device array held by every GPU that
- * loads the library until exit and shared by all calls: calls that overlap on
- * the GPU race.  The first call on a device looks up that array's address; make
- * it before any stream capture.  N must lie in [1, 715827882].  Returns 0, 1 for
- * a size out of range, 2 for a CUDA error (reason on stderr). */
+ * callers that cannot call cudaMalloc at that point (when another allocator
+ * owns the device memory, or in loops that cannot afford the synchronization
+ * cudaMalloc/cudaFree may imply).  Call it from ordinary host code, not from a
+ * stream's host function (it makes CUDA calls).  P (double[N][3], updated in
+ * place), F (double[N][3]), invMass (double[N], or NULL for unit masses) and
+ * twoKE (double[3]: 2KE per dimension) are device pointers; stream is a
+ * cudaStream_t (NULL: default).  The reduction scratch is a fixed 28 KB device
+ * array held by every GPU that loads the library until exit and shared by all
+ * calls: calls that overlap on the GPU race.  The first call on a device looks
+ * up that array's address; make it before any stream capture.  N must lie in
+ * [1, 715827882].  Returns 0, 1 for a size out of range or a NULL P, F or
+ * twoKE, 2 for a CUDA error (reason on stderr). */
 int EmDee_boost_noalloc(double* P, const double* F, const double* invMass, int N, double CP, double CF,
                         double* twoKE, void* stream);
 

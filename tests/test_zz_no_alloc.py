@@ -1,12 +1,16 @@
 """EmDee_boost_noalloc against EmDee_boost, through the C ABI.
 
 EmDee_boost_noalloc serves callers that must not allocate device memory when
-they call it (for example from a cudaLaunchHostFunc callback, or in a loop that
-cannot afford the synchronization cudaMalloc may imply).  It runs the same
-boost + kinetic-energy kernel as EmDee_boost on caller-owned device arrays, with
-its reduction scratch in a fixed device array.  This file is collected last so
-that a run stopping at the first failure has already run every other test; it
-passes both alone in a fresh process and after the rest of the suite.
+they call it: a process whose device memory belongs to another allocator (a
+framework's caching allocator, a pool reserved at start-up), or a loop that
+cannot afford the synchronization cudaMalloc/cudaFree may imply.  It runs the
+same boost + kinetic-energy kernel as EmDee_boost on caller-owned device
+arrays, with its reduction scratch in a fixed device array.  The sizes cover
+one block, the full grid of 1184 blocks with its grid-stride loop (400,000
+atoms: more than 1184 x 256 threads, so every per-block partial slot of the
+scratch is written), and two calls in a row each.  This file is collected last
+so that a run stopping at the first failure has already run every other test;
+it passes both alone in a fresh process and after the rest of the suite.
 """
 import ctypes as C
 import math
@@ -51,10 +55,11 @@ def _system(lib, N, masses):
     return md, types
 
 
-@pytest.mark.parametrize("alpha,masses", [(0.0, [1.0, 1.0]), (0.3, [1.0, 2.5])])
-def test_noalloc_matches_boost_twice(gpu, alpha, masses):
+@pytest.mark.parametrize("N,alpha,masses", [(200, 0.0, [1.0, 1.0]), (5000, 0.0, [1.0, 1.0]),
+                                            (5000, 0.3, [1.0, 2.5]), (400000, 0.3, [1.0, 2.5])])
+def test_noalloc_matches_boost_twice(gpu, N, alpha, masses):
     import torch
-    N, dt = 5000, 0.005
+    dt = 0.005
     md, types = _system(gpu, N, masses)
     rng = np.random.default_rng(5)
     P0 = rng.normal(size=(N, 3))
@@ -91,6 +96,8 @@ def test_noalloc_matches_boost_twice(gpu, alpha, masses):
     gpu.EmDee_destroy(C.byref(md))
 
 
-def test_noalloc_rejects_bad_sizes(gpu):
+def test_noalloc_rejects_bad_arguments(gpu):
     assert gpu.lib.EmDee_boost_noalloc(None, None, None, 0, 1.0, 0.1, None, None) == 1
     assert gpu.lib.EmDee_boost_noalloc(None, None, None, -5, 1.0, 0.1, None, None) == 1
+    # NULL arrays are refused before any CUDA call
+    assert gpu.lib.EmDee_boost_noalloc(None, None, None, 100, 1.0, 0.1, None, None) == 1
