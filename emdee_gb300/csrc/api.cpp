@@ -296,6 +296,7 @@ static void compute_forces_impl(tEmDee* md) {
   bool compute = md->Options.Compute;
   double t0 = wtime();
   flush_pending(s);   // deferred boosts use the forces they were issued with
+  s.keDone = false;   // set by a pair launch that also summed the kinetic energies
   bool rebuild = !s.r0Valid, forcesDone = false;
   if (!rebuild && s.skinReady && s.packReady && s.precision == 0 && s.pairs_exist[s.layer - 1]) {
     // the fused step left the skin decision and the packed positions on the device:
@@ -303,6 +304,7 @@ static void compute_forces_impl(tEmDee* md) {
     // both the decision and the sums
     forcesDone = device_pair_forces(s, compute, true);
     rebuild = !forcesDone;
+    if (rebuild) s.keDone = false;   // the speculative launch returned at once
   } else if (!rebuild) {
     rebuild = s.skinReady ? device_skin_from_step(s) : device_skin_check(s);
   } else {
@@ -537,12 +539,12 @@ tEmDee EmDee_system(int threads, int layers, double rc, double skin, int N, int*
     CK(cudaMalloc(&s->dFree, sizeof(int) * (s->nfree > 0 ? s->nfree : 1)));
     if (s->nfree > 0) CK(cudaMemcpy(s->dFree, s->freeList.data(), sizeof(int) * s->nfree, cudaMemcpyHostToDevice));
   }
-  CK(cudaMallocHost(&s->hResult, sizeof(double) * 48));
+  CK(cudaMallocHost(&s->hResult, sizeof(double) * 64));
   CK(cudaMallocHost(&s->hFlags, sizeof(int) * 16));
-  CK(cudaMalloc(&s->dResult, sizeof(double) * 48));
-  CK(cudaMalloc(&s->dTicket, sizeof(unsigned int) * 8));
-  CK(cudaMemset(s->dTicket, 0, sizeof(unsigned int) * 8));
-  memset(s->hResult, 0, sizeof(double) * 48);
+  CK(cudaMalloc(&s->dResult, sizeof(double) * 64));
+  CK(cudaMalloc(&s->dTicket, sizeof(unsigned int) * 16));
+  CK(cudaMemset(s->dTicket, 0, sizeof(unsigned int) * 16));
+  memset(s->hResult, 0, sizeof(double) * 64);
 
   md.Builds = 0;
   md.DoF = 3 * (N - 1);
@@ -559,6 +561,7 @@ tEmDee EmDee_system(int threads, int layers, double rc, double skin, int N, int*
 
 void EmDee_set_precision(tEmDee md, int mode) {
   System& s = *sys_of(md);
+  s.keSpecValid = false;
   if (mode != 0 && mode != 1) fatal("precision setting", "mode must be 0 (mixed) or 1 (fp64)");
   s.precision = mode;
 }
@@ -612,6 +615,7 @@ void EmDee_destroy(tEmDee* md) {
   cudaFree(s->models.interact);
   cudaFree(s->dPartials);
   cudaFree(s->dKE);
+  cudaFree(s->dKEPair);
   cudaFree(s->dTicket);
   cudaFree(s->dResult);
   cudaFreeHost(s->hResult);
@@ -853,6 +857,7 @@ static bool mirrors_active(const System& s) {
 // src/EmDeeCode.f90:805-925
 void EmDee_upload(tEmDee* md, char* option, double* address) {
   System& s = *sys_of(*md);
+  s.keSpecValid = false;
   char item[257];
   option_string(option, item);
   if (!strcmp(item, "momenta")) sys_of(*md)->npend = 0;   // replaced: pending kicks are moot
@@ -1007,6 +1012,7 @@ void EmDee_download(tEmDee md, char* option, double* address) {
 // it ends, so the caller may read and write it between calls.
 void* EmDee_memory_address(tEmDee md, char* option) {
   System& s = *sys_of(md);
+  s.keSpecValid = false;
   flush_pending(s);
   char item[257];
   option_string(option, item);
@@ -1035,6 +1041,7 @@ void* EmDee_memory_address(tEmDee md, char* option) {
 void EmDee_share_phase_space(tEmDee mdkeep, tEmDee* mdlose) {
   const char* task = "phase space sharing";
   System &keep = *sys_of(mdkeep), &lose = *sys_of(*mdlose);
+  keep.keSpecValid = lose.keSpecValid = false;
   flush_pending(keep);
   flush_pending(lose);
   keep.phaseShared = lose.phaseShared = true;
@@ -1078,6 +1085,7 @@ void EmDee_share_phase_space(tEmDee mdkeep, tEmDee* mdlose) {
 // src/EmDeeCode.f90:929-946
 void EmDee_switch_model_layer(tEmDee* md, int layer) {
   System& s = *sys_of(*md);
+  s.keSpecValid = false;
   flush_pending(s);   // pending kicks belong to the current layer's forces
   if (layer != s.layer) {
     if (layer < 1 || layer > s.nlayers) fatal("model layer switch", "selected layer is out of range");
@@ -1090,6 +1098,7 @@ void EmDee_switch_model_layer(tEmDee* md, int layer) {
 // src/EmDeeCode.f90:950-1020 (serial KISS/ziggurat draws on the host, as the reference)
 void EmDee_random_momenta(tEmDee* md, double kT, bool adjust, int seed) {
   System& s = *sys_of(*md);
+  s.keSpecValid = false;
   s.npend = 0;   // the momenta are replaced
   MirrorScope scope(s);
   int N = s.natoms;
@@ -1185,13 +1194,62 @@ void EmDee_boost(tEmDee* md, double lambda, double alpha, double dt) {
   double CF = phi(alpha * dt) * dt, CP = 1.0 - alpha * CF;
   CF = lambda * CF;
   bool compute = md->Options.Compute;
-  if (lambda != 0.0 && !s.forcesUpToDate[s.layer - 1]) compute_forces_impl(md);
   bool translate = md->Options.Translate, rotate = md->Options.Rotate;
+  const bool deferrable =
+      CP == 1.0 && s.nbodies == 0 && translate && !scope.active && s.initialized && !s.phaseShared;
+  // With energies in mixed precision the kick is deferred as well; only its kinetic
+  // energy is computed now, by a kernel that runs anyway where possible: a boost that
+  // needs new forces gets 2KE from the pair kernel's epilogue, for this kick and for a
+  // second identical one (the next half-kick of a velocity-Verlet loop), and that
+  // second value serves the next boost if P, F and the layer are unchanged by then.
+  if (compute && deferrable && s.precision == 0) {
+    double twoKE[3];
+    const bool stale = lambda != 0.0 && !s.forcesUpToDate[s.layer - 1];
+    const bool spec = s.keSpecValid && !stale && s.keSpecCF == CF;
+    s.keSpecValid = false;
+    bool newSpec = false;
+    if (spec) {
+      for (int d = 0; d < 3; d++) twoKE[d] = s.keSpec[d];
+    } else {
+      if (stale) {
+        s.keMode = 2;
+        s.keCF = CF;
+        compute_forces_impl(md);
+        s.keMode = 0;
+      }
+      if (stale && s.keDone) {
+        for (int d = 0; d < 3; d++) {
+          twoKE[d] = s.hResult[48 + d];
+          s.keSpec[d] = s.hResult[51 + d];
+        }
+        newSpec = true;
+      } else {
+        device_kinetic_pending(s, CF);
+        for (int d = 0; d < 3; d++) twoKE[d] = s.hResult[10 + d];
+      }
+    }
+    if (s.npend == 2) flush_pending(s);   // keeps P plus its pending kicks unchanged
+    s.pendCF[s.npend++] = CF;
+    if (newSpec) {
+      s.keSpecCF = CF;
+      s.keSpecValid = true;
+    }
+    for (int d = 0; d < 3; d++) md->Kinetic.TransPart[d] = 0.5 * twoKE[d];
+    if (rotate) {
+      for (int d = 0; d < 3; d++) md->Kinetic.RotPart[d] = 0.0;
+      md->Kinetic.Rotational = 0.0;
+    }
+    md->Kinetic.Total =
+        md->Kinetic.TransPart[0] + md->Kinetic.TransPart[1] + md->Kinetic.TransPart[2] + md->Kinetic.Rotational;
+    md->Kinetic.UpToDate = true;
+    return;
+  }
+  s.keSpecValid = false;
+  if (lambda != 0.0 && !s.forcesUpToDate[s.layer - 1]) compute_forces_impl(md);
   // Without energies, a plain kick (CP = 1, free atoms) is deferred to the next
   // kernel that touches P: the fused step of EmDee_displace, or a flush.  The
   // arithmetic and its order are unchanged.
-  if (!compute && CP == 1.0 && s.nbodies == 0 && translate && !scope.active && s.initialized && !s.phaseShared &&
-      s.forcesUpToDate[s.layer - 1]) {
+  if (!compute && deferrable && s.forcesUpToDate[s.layer - 1]) {
     if (s.npend == 2) flush_pending(s);
     s.pendCF[s.npend++] = CF;
     md->Kinetic.UpToDate = false;
@@ -1216,6 +1274,7 @@ void EmDee_boost(tEmDee* md, double lambda, double alpha, double dt) {
 // src/EmDeeCode.f90:1069-1103
 void EmDee_displace(tEmDee* md, double lambda, double alpha, double dt) {
   System& s = *sys_of(*md);
+  s.keSpecValid = false;
   MirrorScope scope(s);
   double t0 = wtime(), CR, CP;
   if (alpha != 0.0) {
@@ -1244,6 +1303,7 @@ void EmDee_move(tEmDee* md, double lambda, double alpha, double dt) { EmDee_disp
 
 void EmDee_compute_forces(tEmDee* md) {
   System& s = *sys_of(*md);
+  s.keSpecValid = false;
   MirrorScope scope(s);
   compute_forces_impl(md);
 }
@@ -1254,6 +1314,7 @@ void EmDee_compute_forces(tEmDee* md) {
 // that treat it as input (the replica batches).
 void* EmDee_device_pointer(tEmDee md, const char* item) {
   System& s = *sys_of(md);
+  s.keSpecValid = false;
   flush_pending(s);
   if (!strcmp(item, "coordinates")) return s.dR;
   if (!strcmp(item, "momenta")) return s.dP;
@@ -1264,6 +1325,7 @@ void* EmDee_device_pointer(tEmDee md, const char* item) {
 // src/EmDeeCode.f90:1107-1211
 void EmDee_verlet_step(tEmDee* md, double dt) {
   System& s = *sys_of(*md);
+  s.keSpecValid = false;
   MirrorScope scope(s);
   if (!s.initialized) fatal("verlet step", "system has not been initialized");
   flush_pending(s);

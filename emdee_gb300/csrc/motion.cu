@@ -191,6 +191,57 @@ void device_kinetic(System& s, double* twoKE, const double* src) {
   for (int d = 0; d < 3; d++) twoKE[d] = s.hResult[10 + d];
 }
 
+// 2KE per dimension of P + cf[0] F + ... + cf[NK] F (the pending kicks and one more,
+// applied in order with the fused multiply-adds of k_step_fused) without writing P:
+// the kicks stay deferred.  Flat walk over P[3N] as in k_kinetic.
+template <int NK, bool UNITM>
+__global__ void __launch_bounds__(MOTION_THREADS) k_kinetic_pending(const double* __restrict__ P,
+                                                                    const double* __restrict__ F,
+                                                                    const double* __restrict__ invMass, int N,
+                                                                    double cf0, double cf1, double cf2,
+                                                                    double* partials, unsigned int* ticket,
+                                                                    double* result, double* hostResult) {
+  const size_t n3 = 3 * (size_t)N, stride = (size_t)gridDim.x * blockDim.x;
+  const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double k = 0.0;
+  for (size_t j = g; j < n3; j += stride) {
+    const double f = F[j];
+    double p = fma(cf0, f, P[j]);
+    if (NK >= 1) p = fma(cf1, f, p);
+    if (NK >= 2) p = fma(cf2, f, p);
+    k += UNITM ? p * p : invMass[j / 3] * (p * p);
+  }
+  const int d = (int)(g % 3);
+  double k2[3] = {d == 0 ? k : 0.0, d == 1 ? k : 0.0, d == 2 ? k : 0.0};
+  grid_reduce<3, MOTION_THREADS>(k2, partials, ticket, result + 10, hostResult + 10);
+}
+
+void device_kinetic_pending(System& s, double CF) {
+  const int N = s.natoms;
+  const int blocks = std::min(3 * ((N + 3 * MOTION_THREADS - 1) / (3 * MOTION_THREADS)), 3 * 152);
+  if (s.keCap < blocks) {
+    CK(cudaFree(s.dKE));
+    s.keCap = blocks;
+    CK(cudaMalloc(&s.dKE, sizeof(double) * 3 * blocks));
+  }
+  // the kicks in application order: pending ones first, then CF
+  double c[3] = {CF, 0.0, 0.0};
+  for (int k = 0; k < s.npend; k++) c[k] = s.pendCF[k];
+  c[s.npend] = CF;
+  prof_begin(s, PK_BOOST);
+#define KP_LAUNCH(NK)                                                                                          \
+  (s.unitMass ? k_kinetic_pending<NK, true> : k_kinetic_pending<NK, false>)<<<blocks, MOTION_THREADS, 0,       \
+                                                                              s.stream>>>(                     \
+      s.dP, s.F(), s.dInvMass, N, c[0], c[1], c[2], s.dKE, s.dTicket + 1, s.dResult, s.hResult)
+  if (s.npend == 0) KP_LAUNCH(0);
+  else if (s.npend == 1) KP_LAUNCH(1);
+  else KP_LAUNCH(2);
+#undef KP_LAUNCH
+  CK(cudaGetLastError());
+  prof_end(s, PK_BOOST);
+  CK(cudaStreamSynchronize(s.stream));
+}
+
 void flush_pending(System& s) {
   for (int k = 0; k < s.npend; k++) device_boost(s, 1.0, s.pendCF[k], false);
   s.npend = 0;

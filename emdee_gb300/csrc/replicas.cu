@@ -552,6 +552,7 @@ void* EmDee_replicas_create(int n, tEmDee** systems) {
       if (s.charged[a]) fatal(task, "replicas must carry no charges");
     if (s.natoms > 65535) fatal(task, "replicas are limited to 65535 atoms");
     flush_pending(s);
+    s.keSpecValid = false;   // the batch moves P and F
     CK(cudaStreamSynchronize(s.stream));
     RepDesc d;
     memset(&d, 0, sizeof d);
@@ -627,6 +628,7 @@ void EmDee_replicas_run(void* batch, int steps, double dt, int nprop) {
   if (steps < 0 || nprop < 1) fatal(task, "invalid number of steps");
   for (System* s : B.sys) {
     flush_pending(*s);
+    s->keSpecValid = false;
     CK(cudaStreamSynchronize(s->stream));
   }
   if (B.threads == 0) B.threads = rep_autotune(B, dt, nprop);
@@ -694,6 +696,7 @@ void EmDee_replicas_evaluate(void* batch) {
   Replicas& B = *(Replicas*)batch;
   for (System* s : B.sys) {
     flush_pending(*s);
+    s->keSpecValid = false;
     CK(cudaStreamSynchronize(s->stream));
   }
   if (B.threads == 0) B.threads = 1024;
@@ -735,7 +738,10 @@ static double* rep_item(RepDesc& d, const char* item) {
 
 void EmDee_replicas_gather(void* batch, const char* item, double* dst) {
   Replicas& B = *(Replicas*)batch;
-  for (System* sy : B.sys) flush_pending(*sy);
+  for (System* sy : B.sys) {
+    flush_pending(*sy);
+    sy->keSpecValid = false;
+  }
   size_t off = 0;
   for (int r = 0; r < B.n; r++) {
     const size_t n = (size_t)3 * B.desc[r].N;
@@ -747,7 +753,10 @@ void EmDee_replicas_gather(void* batch, const char* item, double* dst) {
 
 void EmDee_replicas_scatter(void* batch, const char* item, const double* src) {
   Replicas& B = *(Replicas*)batch;
-  for (System* sy : B.sys) flush_pending(*sy);
+  for (System* sy : B.sys) {
+    flush_pending(*sy);
+    sy->keSpecValid = false;
+  }
   size_t off = 0;
   for (int r = 0; r < B.n; r++) {
     const size_t n = (size_t)3 * B.desc[r].N;
@@ -761,7 +770,10 @@ void EmDee_replicas_scatter(void* batch, const char* item, const double* src) {
 // the replicas whose mask entry is nonzero (Metropolis rejections in hybrid Monte Carlo)
 void EmDee_replicas_checkpoint(void* batch) {
   Replicas& B = *(Replicas*)batch;
-  for (System* sy : B.sys) flush_pending(*sy);
+  for (System* sy : B.sys) {
+    flush_pending(*sy);
+    sy->keSpecValid = false;
+  }
   if (B.saved.empty()) {
     for (int r = 0; r < B.n; r++) {
       double* p;
