@@ -242,6 +242,50 @@ void device_kinetic_pending(System& s, double CF) {
   CK(cudaStreamSynchronize(s.stream));
 }
 
+// 2KE per dimension of P + CF F and of P + CF F + CF F (two kicks in sequence, as
+// k_step_fused applies them), P unchanged: 4 fused multiply-adds per component.
+template <bool UNITM>
+__global__ void __launch_bounds__(MOTION_THREADS) k_kinetic_two(const double* __restrict__ P,
+                                                                const double* __restrict__ F,
+                                                                const double* __restrict__ invMass, int N, double cf,
+                                                                double* partials, unsigned int* ticket, double* result,
+                                                                double* hostResult) {
+  const size_t n3 = 3 * (size_t)N, stride = (size_t)gridDim.x * blockDim.x;
+  const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double k1 = 0.0, k2 = 0.0;
+  for (size_t j = g; j < n3; j += stride) {
+    const double f = F[j], p1 = fma(cf, f, P[j]), p2 = fma(cf, f, p1);
+    if (UNITM) {
+      k1 = fma(p1, p1, k1);
+      k2 = fma(p2, p2, k2);
+    } else {
+      const double im = invMass[j / 3];
+      k1 = fma(im * p1, p1, k1);
+      k2 = fma(im * p2, p2, k2);
+    }
+  }
+  const int d = (int)(g % 3);
+  double v[6] = {d == 0 ? k1 : 0.0, d == 1 ? k1 : 0.0, d == 2 ? k1 : 0.0,
+                 d == 0 ? k2 : 0.0, d == 1 ? k2 : 0.0, d == 2 ? k2 : 0.0};
+  grid_reduce<6, MOTION_THREADS>(v, partials, ticket, result + 48, hostResult + 48);
+}
+
+void device_kinetic_two(System& s, double CF) {
+  const int N = s.natoms;
+  const int blocks = std::min(3 * ((N + 3 * MOTION_THREADS - 1) / (3 * MOTION_THREADS)), 3 * 152);
+  if (s.keCap < 2 * blocks) {
+    CK(cudaFree(s.dKE));
+    s.keCap = 2 * blocks;
+    CK(cudaMalloc(&s.dKE, sizeof(double) * 3 * s.keCap));
+  }
+  prof_begin(s, PK_BOOST);
+  (s.unitMass ? k_kinetic_two<true> : k_kinetic_two<false>)<<<blocks, MOTION_THREADS, 0, s.stream>>>(
+      s.dP, s.F(), s.dInvMass, N, CF, s.dKE, s.dTicket + 1, s.dResult, s.hResult);
+  CK(cudaGetLastError());
+  prof_end(s, PK_BOOST);
+  CK(cudaStreamSynchronize(s.stream));
+}
+
 void flush_pending(System& s) {
   for (int k = 0; k < s.npend; k++) device_boost(s, 1.0, s.pendCF[k], false);
   s.npend = 0;

@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <cstdlib>
 
+#include "f32x2.cuh"
 #include "reduce.cuh"
 #include "system.hpp"
 #include "tile.cuh"
@@ -69,14 +70,6 @@ struct PairArgsF {
   const double* R;
   double L;
   int* innerMax;        // largest filtered list
-  // kinetic energies of deferred kicks (keMode 1: 2KE per dimension of P + keCF F,
-  // 2: also of P + keCF F + keCF F), from the forces this launch writes
-  int keMode;
-  double keCF;
-  const double* P;
-  const double* invMass;   // NULL: unit masses
-  double* kePartials;
-  unsigned int* keTicket;
 };
 
 // FP64 distance test of the reference (src/neighbor_lists.f90:247-250) for halo
@@ -102,6 +95,13 @@ __device__ __noinline__ bool refilter_exact(const PairArgsF& A, const int* off, 
 // wrap would bring the sentinel back).
 template <bool COMPUTE, int VAR, int MOD, bool MINIMG, bool COUNT, bool REFILTER>
 __global__ void PAIR_BOUNDS k_pair_mixed(PairArgsF A) {
+  // plain Lennard-Jones (the benchmark's model): two list entries per step of the
+  // inner loop in packed FP32 arithmetic
+#ifdef EMDEE_SCALAR_PAIR   // tuning define: the scalar loop for every variant
+  constexpr bool PACKED = false;
+#else
+  constexpr bool PACKED = VAR == 0 && MOD == NONE && !MINIMG && !COUNT && !REFILTER;
+#endif
   // the flag is 0.0 or 1.0: tested on its bits (an FP64 compare in every thread of
   // every block would queue on the slow FP64 pipe)
   if (A.skip != nullptr && __double_as_longlong(*A.skip) != 0) return;
@@ -128,6 +128,8 @@ __global__ void PAIR_BOUNDS k_pair_mixed(PairArgsF A) {
   NBParams<float> m0 = A.table[0].model;
   if (VAR == 0) m0.modifier = MOD;
   const float sigc = m0.sigsq * A.invw2, eps48 = 2.0f * m0.eps24;
+  const f32x2 sigc2 = pk2(sigc, sigc), eps48_2 = pk2(eps48, eps48), meps24_2 = pk2(-m0.eps24, -m0.eps24),
+              eps4_2 = pk2(m0.eps4, m0.eps4), meps4_2 = pk2(-m0.eps4, -m0.eps4);
   NBParams<float> coul;
   if (VAR == 1) coul = *A.coul;
   const int tb = A.start[t * cells], te = A.start[(t + 1) * cells];
@@ -147,6 +149,7 @@ __global__ void PAIR_BOUNDS k_pair_mixed(PairArgsF A) {
     const uint4* lp = reinterpret_cast<const uint4*>(A.nb) + ((size_t)t * capC * A.tileStride + li);
     const int ti = VAR == 1 ? htype[qi] : 0;
     float fx = 0.f, fy = 0.f, fz = 0.f;
+    f32x2 fx2 = 0ull, fy2 = 0ull, fz2 = 0ull, ep2 = 0ull, wp2 = 0ull;   // PACKED accumulators
     int nIn = 0;
     uint16_t* myIn = REFILTER ? A.nbIn + ((size_t)t * (A.capIn >> 3) * A.tileStride + li) * 8 : nullptr;
     const int ai = REFILTER ? A.orig[si] : 0;
@@ -154,6 +157,29 @@ __global__ void PAIR_BOUNDS k_pair_mixed(PairArgsF A) {
     for (int c = sub; c < nch; c += tpa) {
       const uint4 nxt = (c + tpa < nch) ? __ldcs(lp + (size_t)(c + tpa) * A.tileStride) : cur;
       const unsigned w[4] = {cur.x, cur.y, cur.z, cur.w};
+      if (PACKED) {
+        // entries 2k (low half of word k) and 2k + 1 (high half) side by side;
+        // entries beyond the cut-off (and sentinels) get a zero reciprocal, which
+        // zeroes their energy, virial and force without a branch
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+          const float4 pa = hpos[w[k] & 0xFFFF], pb = hpos[w[k] >> 16];
+          const f32x2 dx = pk2(pi.x - pa.x, pi.x - pb.x), dy = pk2(pi.y - pa.y, pi.y - pb.y),
+                      dz = pk2(pi.z - pa.z, pi.z - pb.z);
+          const float2 r2 = up2(fma2(dz, dz, fma2(dy, dy, mul2(dx, dx))));
+          const f32x2 inv = pk2(r2.x < A.rc2 ? Ops<float>::rcp(r2.x) : 0.f, r2.y < A.rc2 ? Ops<float>::rcp(r2.y) : 0.f);
+          const f32x2 sr2 = mul2(sigc2, inv), sr6 = mul2(mul2(sr2, sr2), sr2);
+          const f32x2 W = mul2(sr6, fma2(eps48_2, sr6, meps24_2));
+          if (COMPUTE) ep2 = fma2(sr6, fma2(eps4_2, sr6, meps4_2), ep2);
+          wp2 = add2(wp2, W);
+          const f32x2 sc = mul2(W, inv);
+          fx2 = fma2(sc, dx, fx2);
+          fy2 = fma2(sc, dy, fy2);
+          fz2 = fma2(sc, dz, fz2);
+        }
+        cur = nxt;
+        continue;
+      }
 #pragma unroll
       for (int e = 0; e < 8; e++) {
         if (MINIMG && c * 8 + e >= n) break;
@@ -214,6 +240,14 @@ __global__ void PAIR_BOUNDS k_pair_mixed(PairArgsF A) {
       A.countIn[si] = nIn;
       longestIn = max(longestIn, nIn);
     }
+    if (PACKED) {
+      const float2 a = up2(fx2), b = up2(fy2), c = up2(fz2), ee = up2(ep2), ww = up2(wp2);
+      fx = a.x + a.y;
+      fy = b.x + b.y;
+      fz = c.x + c.y;
+      if (COMPUTE) Ep += ee.x + ee.y;
+      Wp += ww.x + ww.y;
+    }
     for (int o = tpa >> 1; o > 0; o >>= 1) {
       fx += __shfl_xor_sync(gmask, fx, o);
       fy += __shfl_xor_sync(gmask, fy, o);
@@ -229,28 +263,6 @@ __global__ void PAIR_BOUNDS k_pair_mixed(PairArgsF A) {
   if (REFILTER) {   // one atomic per warp
     longestIn = __reduce_max_sync(0xffffffffu, longestIn);
     if ((threadIdx.x & 31) == 0) atomicMax(A.innerMax, longestIn);
-  }
-  if (!COUNT && !REFILTER && A.keMode != 0) {
-    // 2KE per dimension of the momenta after one and two kicks by the forces just
-    // written (the kicks stay deferred: P is not written).  Each thread reads back
-    // the forces it stored itself, so the FP64 sums are live only here.
-    double kv[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-    const double cf = A.keCF;
-    for (int li = threadIdx.x >> tpaShift; li < te - tb; li += blockDim.x >> tpaShift) {
-      if (sub != 0) continue;
-      const int ai = A.orig[tb + li];
-      const double im = A.invMass ? A.invMass[ai] : 1.0;
-#pragma unroll
-      for (int d = 0; d < 3; d++) {
-        const double f = A.F[3 * (size_t)ai + d], p1 = fma(cf, f, A.P[3 * (size_t)ai + d]);
-        kv[d] += im * (p1 * p1);
-        if (A.keMode == 2) {
-          const double p2 = fma(cf, f, p1);
-          kv[3 + d] += im * (p2 * p2);
-        }
-      }
-    }
-    grid_reduce<6, PAIR_MAX_THREADS>(kv, A.kePartials, A.keTicket, A.result + 48, A.hostResult + 48);
   }
   // each pair is visited from both atoms: halve the sums.  Sums that are zero by
   // construction (energies without COMPUTE, Coulomb terms of VAR 0, the count
@@ -326,12 +338,6 @@ static size_t pair_args(System& s, bool useInRc, double rc2scaled, bool general,
   A.R = nullptr;
   A.L = L;
   A.innerMax = nullptr;
-  A.keMode = 0;
-  A.keCF = 0.0;
-  A.P = s.dP;
-  A.invMass = s.unitMass ? nullptr : s.dInvMass;
-  A.kePartials = nullptr;
-  A.keTicket = s.dTicket + 8;
   size_t smem = (size_t)(g.maxHalo + 1) * sizeof(float4) + sizeof(int) * (3 * g.haloCells + 1);
   if (general) smem += sizeof(PairEntry<float>) * s.ntypes * s.ntypes + g.maxHalo + 17;
   return smem;
@@ -344,17 +350,6 @@ void device_pair_forces_mixed(System& s, bool compute, bool useInRc, double rc2s
   PairArgsF A;
   const size_t smem = pair_args(s, useInRc, rc2scaled, variant != 0, A);
   const bool mi = g.M == 5;
-  if (variant != 2 && s.keMode != 0) {   // kinetic energies of the deferred kick(s)
-    if (s.kePairCap < g.nTiles) {
-      CK(cudaFree(s.dKEPair));
-      s.kePairCap = g.nTiles;
-      CK(cudaMalloc(&s.dKEPair, sizeof(double) * 6 * s.kePairCap));
-    }
-    A.keMode = s.keMode;
-    A.keCF = s.keCF;
-    A.kePartials = s.dKEPair;
-    s.keDone = true;
-  }
   // Threads per atom: systems too small to fill the GPU with one thread per atom
   // (fewer than ~2048 threads per SM) and with long lists (more than 48 entries per
   // thread) split each list over 2, 4 or 8 threads of a warp (general variant only,

@@ -236,17 +236,12 @@ struct System {
   // FP32 positions of the new coordinates (valid until R or the lists change)
   int npend = 0;
   double pendCF[2] = {0.0, 0.0};
-  // kinetic energy of deferred kicks with energies (mixed precision, free atoms):
-  // keMode asks the next pair launch for 2KE of P + keCF F (1) and also of
-  // P + 2 keCF F (2, the next half-kick of a velocity-Verlet loop, kept as keSpec
-  // until P, F or the layer change); the launch sets keDone
-  int keMode = 0;
-  double keCF = 0.0;
-  bool keDone = false;
+  // kinetic energy of deferred kicks with energies (mixed precision, free atoms): a
+  // boost that needed new forces also sums 2KE of P + 2 CF F, the momenta after the
+  // next identical half-kick of a velocity-Verlet loop, kept as keSpec until P, F
+  // or the layer change
   bool keSpecValid = false;
   double keSpecCF = 0.0, keSpec[3] = {0.0, 0.0, 0.0};
-  double* dKEPair = nullptr;   // per tile: 6 partial sums of the pair kernel's kinetic energies
-  int kePairCap = 0;
   bool skinReady = false, packReady = false;
   bool phaseShared = false;   // R/P aliased with another system (no deferral then)
   const double* pairSkip = nullptr;   // device rebuild flag the mixed pair kernel checks first
@@ -270,8 +265,7 @@ struct System {
   // (translational) per dimension, [13..15] 2KE (rotational), [16..21] body 2KE sums
   // (translational, rotational) of one body kernel, [22] k-space energy, [24..32] and
   // [34..38] sums of the Verlet step (bodies, free atoms), [40..41] coverage test of
-  // the two-level lists, [48..53] 2KE per dimension after one and after two kicks of
-  // keCF (pair kernel epilogue)
+  // the two-level lists, [48..53] 2KE per dimension after one and after two kicks
   double* hResult = nullptr;
   double* dResult = nullptr;
 
@@ -327,6 +321,9 @@ void device_boost(System& s, double CP, double CF, bool kinetic);
 // 2KE per dimension (hResult[10..12]) of the momenta after the pending kicks and one
 // more kick of CF, without changing P (free atoms, mixed precision); synchronizes
 void device_kinetic_pending(System& s, double CF);
+// 2KE per dimension after one (hResult[48..50]) and after two (hResult[51..53]) kicks
+// of CF, no pending kicks, P unchanged (free atoms, mixed precision); synchronizes
+void device_kinetic_two(System& s, double CF);
 // 2KE per dimension of the momenta, free atoms only (no bodies); src: the momenta are
 // read from there (a device-accessible pointer to the caller's pinned buffer) and
 // stored into P on the way

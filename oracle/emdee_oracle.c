@@ -1970,6 +1970,7 @@ void EmDee_share_phase_space(tEmDee mdkeep, tEmDee* mdlose) {   /* src/EmDeeCode
   }
   lose->R = keep->R;
   lose->P = keep->P;
+  lose->body = keep->body;   /* lose%body => keep%body (src/EmDeeCode.f90:261) */
   lose->Lbox = keep->Lbox;
   mdlose->Kinetic.Total = mdkeep.Kinetic.Total;
   for (int d = 0; d < 3; d++) {

@@ -119,6 +119,10 @@ def test_config0_mixed_1000_steps_shadowed(gpu, oracle):
     configuration of the GPU trajectory; its own skin check, run on the same
     coordinates, must rebuild at the same steps.
 
+    The virial's error is taken relative to max(|W|, 3 N kT): the virial total
+    passes near zero along this trajectory (attraction and repulsion cancel), so
+    its plain relative error is not a measure of the arithmetic.
+
     FP32 distances decide the cut-off test at force time (the lists themselves
     are exact): a pair within ~1e-7 (relative) of rc can land on the other side of
     it than in FP64.  lj_cut is discontinuous at rc, so one such pair moves this
@@ -145,7 +149,10 @@ def test_config0_mixed_1000_steps_shadowed(gpu, oracle):
         assert dev.Builds == shadow.Builds, step
 
         def errors(F, U, W):
-            return np.array([rel_rms(Fd, F), abs(dev.Energy.Potential - U) / abs(U), abs(dev.Virial.Total - W) / abs(W)])
+            # the virial enters the pressure next to the kinetic term 2K = 3 N kT; near
+            # a cancelling total (|W| << 3 N kT) its error is measured against that term
+            return np.array([rel_rms(Fd, F), abs(dev.Energy.Potential - U) / abs(U),
+                             abs(dev.Virial.Total - W) / max(abs(W), 3 * N * 1.5)])
 
         bounds = np.array([FORCE_RMS_MIXED, ENERGY_REL_MIXED, VIRIAL_REL_MIXED])
         e = errors(Fo, Uo, Wo)
