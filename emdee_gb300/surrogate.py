@@ -338,12 +338,17 @@ def _gather_forces(chains):
     return chains.gather("F")
 
 
-def train(model, Rs, Es, Fs, epochs, lr, batch, seed, wE=1.0, wF=1.0, log=None):
-    """Adam on energy + force matching (learning rate lr, then lr / 5 for the last 40 %
-    of the epochs); the model's chain count is the batch size."""
+def train(model, Rs, Es, Fs, epochs, lr, batch, seed, wE=1.0, wF=1.0, log=None, lr_min=None):
+    """Adam on energy + force matching.  The learning rate follows a cosine from lr to
+    lr_min (default lr / 50) over all steps; the model's chain count is the batch size.
+    Returns the mean (energy, force) loss of every epoch."""
     S = Rs.shape[0]
     g = torch.Generator(device="cuda").manual_seed(seed)
+    lr_min = lr / 50.0 if lr_min is None else lr_min
+    nb_epoch = S // batch
+    total = max(1, epochs * nb_epoch)
     history = []
+    step = 0
     for ep in range(epochs):
         perm = torch.randperm(S, device="cuda", generator=g)
         lE = lF = 0.0
@@ -354,7 +359,8 @@ def train(model, Rs, Es, Fs, epochs, lr, batch, seed, wE=1.0, wF=1.0, log=None):
             E = Es[idx].contiguous()
             F = Fs[idx].double().contiguous()
             a, c, _ = model.gradient(R, E, F, wE, wF)
-            model.adam(lr * (0.2 if ep >= 0.6 * epochs else 1.0))
+            model.adam(lr_min + 0.5 * (lr - lr_min) * (1.0 + math.cos(math.pi * step / total)))
+            step += 1
             lE += a
             lF += c
             nb += 1

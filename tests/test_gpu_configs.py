@@ -125,7 +125,8 @@ def test_config0_mixed_1000_steps_shadowed(gpu, oracle):
 
     FP32 distances decide the cut-off test at force time (the lists themselves
     are exact): a pair within ~1e-7 (relative) of rc can land on the other side of
-    it than in FP64.  lj_cut is discontinuous at rc, so one such pair moves this
+    it than in FP64, from one of its atoms or from both (each atom's list tests the
+    pair in its own tile frame).  lj_cut is discontinuous at rc, so one such pair moves this
     4000-atom force field by ~2.5e-5 RMS and the energy by |E(rc)| = 0.016 (at
     1M atoms the same flip is 3e-7 RMS).  A step outside the bounds must be
     explained exactly by flips of such boundary pairs (found from the oracle's
@@ -159,17 +160,20 @@ def test_config0_mixed_1000_steps_shadowed(gpu, oracle):
         if not np.all(e < bounds):
             # try every in/out assignment of the boundary pairs
             cand = boundary_flips(oracle, shadow, R, L)
-            assert 0 < len(cand) <= 4, (step, e, len(cand))
-            # each boundary pair: as the oracle decided it (0), added (+1) or removed (-1)
+            assert 0 < len(cand) <= 3, (step, e, len(cand))
+            # each boundary pair, from each of its two atoms' lists (full lists: the
+            # pair is tested twice, in two tile frames): as the oracle decided it (0),
+            # added (+1) or removed (-1); each side carries half the energy and virial
             best = None
-            for code in range(1, 3 ** len(cand)):
+            for code in range(1, 9 ** len(cand)):
                 F, U, W = Fo.copy(), Uo, Wo
                 for b, (i, j, f, Ep, Wp) in enumerate(cand):
-                    s = (0.0, 1.0, -1.0)[code // 3 ** b % 3]
-                    F[i] += s * f
-                    F[j] -= s * f
-                    U += s * Ep
-                    W += s * Wp
+                    si = (0.0, 1.0, -1.0)[code // 9 ** b % 3]
+                    sj = (0.0, 1.0, -1.0)[code // 9 ** b // 3 % 3]
+                    F[i] += si * f
+                    F[j] -= sj * f
+                    U += 0.5 * (si + sj) * Ep
+                    W += 0.5 * (si + sj) * Wp
                 ee = errors(F, U, W)
                 if best is None or np.max(ee / bounds) < np.max(best / bounds):
                     best = ee

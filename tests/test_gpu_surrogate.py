@@ -180,3 +180,33 @@ def test_training_and_hmc(gpu):
     m.close()
     hm.close()
     ch.close()
+
+
+def test_trained_surrogate_accepts(gpu):
+    """A surrogate trained on plain-MD data of a small mixture (512 atoms, 16
+    chains) proposes trajectories that the exact Hamiltonian accepts: acceptance
+    above zero for 2- and 5-step trajectories, held-out force error below 30 % of
+    the RMS force.  Prints acceptance and ESS/s of surrogate and plain HMC."""
+    from emdee_gb300.surrogate import (Chains, ess, force_rmse, generate_data, plain_hmc, surrogate_hmc,
+                                       train)
+    N, C, dt, kT = 512, 16, 0.004, 0.8
+    ch = Chains(gpu, C, N, 41)
+    Rs, Es, Fs = generate_data(ch, 1600, 25, dt, kT, 42, burn=400)
+    m = model(gpu, 8, N, ch.L, ch.types)
+    m.init_params(43, float(Es.mean()) / N)
+    train(m, Rs[:1440], Es[:1440], Fs[:1440], 15, 3e-3, 8, 44)
+    rmse = force_rmse(m, Rs[1440:], Fs[1440:], 8)
+    rms = float(Fs[1440:].double().pow(2).mean().sqrt())
+    print("held-out force RMSE %.3f of RMS force %.3f (%.1f %%)" % (rmse, rms, 100 * rmse / rms))
+    assert rmse < 0.3 * rms
+    hm = model(gpu, C, N, ch.L, ch.types)
+    hm.set_params(m.get_params())
+    for steps in (2, 5):
+        U, acc, secs = plain_hmc(ch, 30, steps, dt, kT, 45 + steps)
+        U2, acc2, secs2, far = surrogate_hmc(ch, hm, 30, steps, dt, kT, 46 + steps)
+        print("%d-step trajectories: acceptance plain %.3f surrogate %.3f; ESS/s plain %.1f surrogate %.1f"
+              % (steps, acc, acc2, ess(U[:, 6:]) / secs, ess(U2[:, 6:]) / secs2))
+        assert acc2 > 0.0 and far == 0
+    m.close()
+    hm.close()
+    ch.close()
