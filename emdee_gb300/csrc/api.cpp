@@ -296,7 +296,6 @@ static void compute_forces_impl(tEmDee* md) {
   bool compute = md->Options.Compute;
   double t0 = wtime();
   flush_pending(s);   // deferred boosts use the forces they were issued with
-  s.keDone = false;   // set by a pair launch that also sums the kinetic energies
   bool rebuild = !s.r0Valid, forcesDone = false;
   if (!rebuild && s.skinReady && s.packReady && s.precision == 0 && s.pairs_exist[s.layer - 1]) {
     // the fused step left the skin decision and the packed positions on the device:
@@ -304,7 +303,6 @@ static void compute_forces_impl(tEmDee* md) {
     // both the decision and the sums
     forcesDone = device_pair_forces(s, compute, true);
     rebuild = !forcesDone;
-    if (rebuild) s.keDone = false;   // the speculative launch returned at once
   } else if (!rebuild) {
     rebuild = s.skinReady ? device_skin_from_step(s) : device_skin_check(s);
   } else {
@@ -615,7 +613,6 @@ void EmDee_destroy(tEmDee* md) {
   cudaFree(s->models.interact);
   cudaFree(s->dPartials);
   cudaFree(s->dKE);
-  cudaFree(s->dKEPair);
   cudaFree(s->dTicket);
   cudaFree(s->dResult);
   cudaFreeHost(s->hResult);
@@ -1198,10 +1195,12 @@ void EmDee_boost(tEmDee* md, double lambda, double alpha, double dt) {
   const bool deferrable =
       CP == 1.0 && s.nbodies == 0 && translate && !scope.active && s.initialized && !s.phaseShared;
   // With energies in mixed precision the kick is deferred as well and only its kinetic
-  // energy is computed now, without writing P.  A boost that needs new forces gets 2KE
-  // from the pair kernel's epilogue, for this kick and for a second identical one (the
-  // next half-kick of a velocity-Verlet loop); that second value serves the next boost
-  // if P, F and the layer are unchanged by then.  Otherwise a pass over P and F sums it.
+  // energy is computed now, by a pass that reads P and F and writes nothing.  A boost
+  // that needed new forces sums 2KE for this kick and for a second identical one (the
+  // next half-kick of a velocity-Verlet loop) in the same pass; that second value
+  // serves the next boost if P, F and the layer are unchanged by then.  (Summing them
+  // in the pair kernel's epilogue was measured slower: its FP64 work queues on
+  // GB300's narrow FP64 pipe at the end of every block.)
   if (compute && deferrable && s.precision == 0) {
     double twoKE[3];
     const bool stale = lambda != 0.0 && !s.forcesUpToDate[s.layer - 1];
@@ -1211,14 +1210,9 @@ void EmDee_boost(tEmDee* md, double lambda, double alpha, double dt) {
     if (spec) {
       for (int d = 0; d < 3; d++) twoKE[d] = s.keSpec[d];
     } else {
-      if (stale) {   // applies the pending kicks first
-        s.keMode = 1;
-        s.keCF = CF;
-        compute_forces_impl(md);
-        s.keMode = 0;
-        if (!s.keDone && s.npend == 0) device_kinetic_two(s, CF);   // a launch without the sums
-      }
+      if (stale) compute_forces_impl(md);   // applies the pending kicks first
       if (stale && s.npend == 0) {
+        device_kinetic_two(s, CF);
         for (int d = 0; d < 3; d++) {
           twoKE[d] = s.hResult[48 + d];
           s.keSpec[d] = s.hResult[51 + d];

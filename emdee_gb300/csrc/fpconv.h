@@ -30,27 +30,5 @@ EMD_HD_INLINE bool d2f_normal(unsigned long long b) {
   return e >= 1 && e <= 253;
 }
 
-#ifdef __CUDACC__
-// x (finite, |x| within the normal float range or zero) as hi + lo, two floats with
-// 48 significant bits together: hi the rounded value, lo the rounded remainder.
-// Integer operations and one FP64 subtraction.
-__device__ __forceinline__ void d2ff(double x, float& hi, float& lo) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  if (!d2f_normal(b)) {   // zero or out of range for the split: plain conversion
-    hi = (float)x;
-    lo = 0.f;
-    return;
-  }
-  const unsigned int hb = d2f_bits(b);
-  hi = __uint_as_float(hb);
-  // the float hi as a double, exactly (normal float: rebias the exponent)
-  const unsigned long long s = (unsigned long long)(hb & 0x80000000u) << 32;
-  const unsigned long long e = (unsigned long long)(((hb >> 23) & 255u) - 127u + 1023u) << 52;
-  const unsigned long long m = (unsigned long long)(hb & 0x7FFFFFu) << 29;
-  const double r = x - __longlong_as_double((long long)(s | e | m));   // exact
-  const unsigned long long rb = (unsigned long long)__double_as_longlong(r);
-  lo = d2f_normal(rb) ? __uint_as_float(d2f_bits(rb)) : (float)r;
-}
-#endif
 
 }  // namespace emdee

@@ -669,124 +669,6 @@ __global__ void BUILD_BOUNDS k_build(BuildArgs A) {
   }
 }
 
-// Cell-parallel build (one atom type, no exclusions, bodies or layers, M > 5): a
-// warp takes one cell of the tile at a time.  The candidates of the cell's atoms
-// are the atoms of the 25 stencil rows (rz, ry) around it, each row 5 consecutive
-// halo cells sorted along x; the warp walks their concatenation 32 candidates at a
-// time (one per lane) and tests each against every atom of the cell, so every lane
-// has work whatever the row lengths.  Accepted candidates are appended with a
-// ballot: their order in each list is (row, ascending halo index), the order of
-// k_build, and so are the lists, entry for entry.
-static const int BUILD_CELL_THREADS = 256;
-static const int BUILD_CELL_WARPS = BUILD_CELL_THREADS / 32;
-
-__global__ void __launch_bounds__(BUILD_CELL_THREADS) k_build_cells(BuildArgs A) {
-  extern __shared__ __align__(16) unsigned char sraw[];
-  __shared__ int ws[33];
-  __shared__ int rowStart[BUILD_CELL_WARPS][25], rowPre[BUILD_CELL_WARPS][26];
-  const TileGeom g = A.g;
-  const int t = blockIdx.x, cells = g.TB * g.TB * g.TB;
-  float4* hpos = (float4*)sraw;
-  int* hslot = (int*)(hpos + A.haloCap + 1);
-  int* off = hslot + A.haloCap + 1;
-  int* cst = off + g.haloCells + 1;
-  int* hxyz = cst + g.haloCells;
-  const int haloCount = halo_layout(g, t, A.tab, A.start, off, cst, hxyz, ws);
-  {
-    // sizes taken from the previous build: a tile or halo that outgrew them is
-    // reported (the host re-sizes and builds again) before anything is staged
-    const int tileCount = A.start[(t + 1) * cells] - A.start[t * cells];
-    if (tileCount > A.tileStride || haloCount > A.haloCap) {
-      if (threadIdx.x == 0) atomicOr(A.maxCount + 1, 1);
-      return;
-    }
-  }
-  {   // the layout, saved for the force kernels until the next build
-    int* dst = A.layout + (size_t)t * (2 * g.haloCells + 1);
-    for (int h = threadIdx.x; h <= g.haloCells; h += blockDim.x) dst[h] = off[h];
-    for (int h = threadIdx.x; h < g.haloCells; h += blockDim.x) dst[g.haloCells + 1 + h] = cst[h];
-  }
-  if (threadIdx.x == 0) hpos[A.haloCap] = make_float4(1e9f, 1e9f, 1e9f, 0.f);
-  stage_frame_flat(g, off, cst, hxyz, A.pos4, hpos, hslot, (uint8_t*)nullptr, A.type8);
-  __syncthreads();
-  const bool none = !A.interact[0];   // the only type pair does not interact: empty lists
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, HW = g.HW;
-  const int tb = A.start[t * cells], capC = A.cap >> 3, chunkStride = A.tileStride * 8;
-  const unsigned lt = (1u << lane) - 1u;
-  int* rs = rowStart[warp];
-  int* rp = rowPre[warp];
-  for (int c = warp; c < cells; c += BUILD_CELL_WARPS) {
-    const int rank = t * cells + c, s0 = A.start[rank], ni = A.start[rank + 1] - s0;
-    if (ni == 0) continue;
-    const int lx = c % g.TB, ly = (c / g.TB) % g.TB, lz = c / (g.TB * g.TB);
-    const int q0 = off[(lx + 2) + HW * ((ly + 2) + HW * (lz + 2))];   // halo index of the cell's first atom
-    // rows: lane r < 25 is row (rz, ry) = (r / 5 - 2, r % 5 - 2); exclusive prefix of their lengths
-    __syncwarp();   // the previous cell's row table has been read by every lane
-    int len = 0;
-    if (lane < 25) {
-      const int h0 = lx + HW * ((ly + lane % 5) + HW * (lz + lane / 5));
-      rs[lane] = off[h0];
-      len = off[h0 + 5] - off[h0];
-    }
-    int incl = len;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += y;
-    }
-    if (lane < 25) rp[lane + 1] = incl;
-    if (lane == 0) rp[0] = 0;
-    const int total = none ? 0 : __shfl_sync(0xffffffffu, incl, 24);
-    __syncwarp();
-    // the cell's atoms two at a time: positions, atom indices and list counts in
-    // registers (counts are warp-uniform: every lane adds the same ballot counts)
-    for (int k0 = 0; k0 < ni; k0 += 2) {
-      const bool two = k0 + 1 < ni;
-      const float4 pa = hpos[q0 + k0], pb = two ? hpos[q0 + k0 + 1] : make_float4(1e9f, 1e9f, 1e9f, 0.f);
-      const int aa = A.orig[s0 + k0], ab = two ? A.orig[s0 + k0 + 1] : 0;
-      const int la = s0 - tb + k0;   // tile-local index of the first atom
-      int ca = 0, cb = 0;
-      int r = 0;
-      for (int base = 0; base < total; base += 32) {
-        const int f = base + lane;
-        const bool valid = f < total;
-        while (r < 24 && rp[r + 1] <= f) r++;
-        const int q = valid ? rs[r] + (f - rp[r]) : A.haloCap;
-        const float4 pj = hpos[q];
-        const float xa = pa.x - pj.x, ya = pa.y - pj.y, za = pa.z - pj.z;
-        const float xb = pb.x - pj.x, yb = pb.y - pj.y, zb = pb.z - pj.z;
-        const float ra = xa * xa + ya * ya + za * za, rb = xb * xb + yb * yb + zb * zb;
-        bool acca = valid && ra < A.hi2 && q != q0 + k0;
-        bool accb = valid && two && rb < A.hi2 && q != q0 + k0 + 1;
-        // within the band around (rc + skin)^2: the reference's FP64 test
-        if (acca && !(ra < A.lo2)) acca = exact_inside(A.R, A.L, aa, A.orig[hslot[q]], A.thr);
-        if (accb && !(rb < A.lo2)) accb = exact_inside(A.R, A.L, ab, A.orig[hslot[q]], A.thr);
-        const unsigned ma = __ballot_sync(0xffffffffu, acca), mb = __ballot_sync(0xffffffffu, accb);
-        if (acca) {
-          const int pos = ca + __popc(ma & lt);
-          if (pos < A.cap) A.nb[nb_index(t, capC, A.tileStride, la, pos)] = (uint16_t)q;
-        }
-        if (accb) {
-          const int pos = cb + __popc(mb & lt);
-          if (pos < A.cap) A.nb[nb_index(t, capC, A.tileStride, la + 1, pos)] = (uint16_t)q;
-        }
-        ca += __popc(ma);
-        cb += __popc(mb);
-      }
-      // lane 0 and 1 finish the two lists: sentinel padding of the last chunk, counts
-      if (lane < (two ? 2 : 1)) {
-        const int si = s0 + k0 + lane, li = si - tb, cnt = lane == 0 ? ca : cb;
-        A.selfIdx[si] = (uint16_t)(q0 + k0 + lane);
-        uint16_t* myList = A.nb + ((size_t)t * capC * A.tileStride + li) * 8;
-        for (int p = cnt; p < A.cap && (p & 7); p++) myList[(p >> 3) * chunkStride + (p & 7)] = (uint16_t)A.haloCap;
-        A.nbCount[si] = cnt;
-        A.nbInner[si] = cnt;
-        atomicMax(A.maxCount, cnt);
-      }
-    }
-  }
-}
-
 template <typename T>
 static void grow(T*& p, size_t& have, size_t need) {
   if (have >= need) return;
@@ -989,15 +871,11 @@ static bool build_lists(System& s, bool reuse) {
     A.tpaShift = shift;
   }
   const bool split = A.tpa > 1;
-  // the cell-parallel build serves the plain case (EMDEE_BUILD=thread keeps the thread-per-atom one)
-  static const bool threadBuild = getenv("EMDEE_BUILD") && !strcmp(getenv("EMDEE_BUILD"), "thread");
-  const bool cellBuild = !general && !A.minimg && !threadBuild;
-  auto kb = cellBuild ? k_build_cells : split ? (general ? (A.minimg ? k_build<true, true, true> : k_build<true, false, true>)
+  auto kb = split ? (general ? (A.minimg ? k_build<true, true, true> : k_build<true, false, true>)
                              : (A.minimg ? k_build<false, true, true> : k_build<false, false, true>))
                   : (general ? (A.minimg ? k_build<true, true, false> : k_build<true, false, false>)
                              : (A.minimg ? k_build<false, true, false> : k_build<false, false, false>));
-  const int buildThreads = cellBuild ? std::max(halo_min_threads(geo), BUILD_CELL_THREADS)
-                         : std::max(halo_min_threads(geo), split ? std::min(BUILD_THREADS_SPLIT, g.tileStride * A.tpa)
+  const int buildThreads = std::max(halo_min_threads(geo), split ? std::min(BUILD_THREADS_SPLIT, g.tileStride * A.tpa)
                                                                  : std::min(BUILD_THREADS, std::max(32, g.tileStride)));
   CK(cudaFuncSetAttribute(kb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
 #ifdef EMDEE_MAX_CARVEOUT

@@ -70,15 +70,6 @@ struct PairArgsF {
   const double* R;
   double L;
   int* innerMax;        // largest filtered list
-  // kinetic energies of deferred kicks: with keMode != 0, 2KE per dimension of
-  // P + keCF F and of P + keCF F + keCF F from the forces this launch writes
-  // (result[48..53]); FP64 per thread, float-float from there on
-  int keMode;
-  double keCF;
-  const double* P;
-  const double* invMass;   // NULL: unit masses
-  float2* kePartials;
-  unsigned int* keTicket;
 };
 
 // FP64 distance test of the reference (src/neighbor_lists.f90:247-250) for halo
@@ -273,27 +264,6 @@ __global__ void PAIR_BOUNDS k_pair_mixed(PairArgsF A) {
     longestIn = __reduce_max_sync(0xffffffffu, longestIn);
     if ((threadIdx.x & 31) == 0) atomicMax(A.innerMax, longestIn);
   }
-  if (!COUNT && !REFILTER && A.keMode != 0) {
-    // each thread reads back the forces it stored (its own writes) and the momenta;
-    // FP64 only per thread: GB300's FP64 pipe is too narrow for FP64 reductions here
-    double kv[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-    const double cf = A.keCF;
-    for (int li = threadIdx.x >> tpaShift; li < te - tb; li += blockDim.x >> tpaShift) {
-      if (sub != 0) continue;
-      const int ai = A.orig[tb + li];
-      const double im = A.invMass ? A.invMass[ai] : 1.0;
-#pragma unroll
-      for (int d = 0; d < 3; d++) {
-        const double f = A.F[3 * (size_t)ai + d], p1 = fma(cf, f, A.P[3 * (size_t)ai + d]), p2 = fma(cf, f, p1);
-        kv[d] = fma(im * p1, p1, kv[d]);
-        kv[3 + d] = fma(im * p2, p2, kv[3 + d]);
-      }
-    }
-    float kh[6], kl[6];
-#pragma unroll
-    for (int q = 0; q < 6; q++) d2ff(kv[q], kh[q], kl[q]);
-    grid_reduce_ff2<6, PAIR_MAX_THREADS>(kh, kl, A.kePartials, A.keTicket, A.result + 48, A.hostResult + 48);
-  }
   // each pair is visited from both atoms: halve the sums.  Sums that are zero by
   // construction (energies without COMPUTE, Coulomb terms of VAR 0, the count
   // without COUNT) skip the reduction.
@@ -368,12 +338,6 @@ static size_t pair_args(System& s, bool useInRc, double rc2scaled, bool general,
   A.R = nullptr;
   A.L = L;
   A.innerMax = nullptr;
-  A.keMode = 0;
-  A.keCF = 0.0;
-  A.P = s.dP;
-  A.invMass = s.unitMass ? nullptr : s.dInvMass;
-  A.kePartials = nullptr;
-  A.keTicket = s.dTicket + 8;
   size_t smem = (size_t)(g.maxHalo + 1) * sizeof(float4) + sizeof(int) * (3 * g.haloCells + 1);
   if (general) smem += sizeof(PairEntry<float>) * s.ntypes * s.ntypes + g.maxHalo + 17;
   return smem;
@@ -386,17 +350,6 @@ void device_pair_forces_mixed(System& s, bool compute, bool useInRc, double rc2s
   PairArgsF A;
   const size_t smem = pair_args(s, useInRc, rc2scaled, variant != 0, A);
   const bool mi = g.M == 5;
-  if (variant != 2 && s.keMode != 0) {   // kinetic energies of the deferred kicks
-    if (s.kePairCap < g.nTiles) {
-      CK(cudaFree(s.dKEPair));
-      s.kePairCap = g.nTiles;
-      CK(cudaMalloc(&s.dKEPair, sizeof(float2) * 6 * s.kePairCap));
-    }
-    A.keMode = s.keMode;
-    A.keCF = s.keCF;
-    A.kePartials = s.dKEPair;
-    s.keDone = true;
-  }
   // Threads per atom: systems too small to fill the GPU with one thread per atom
   // (fewer than ~2048 threads per SM) and with long lists (more than 48 entries per
   // thread) split each list over 2, 4 or 8 threads of a warp (general variant only,

@@ -237,15 +237,9 @@ struct System {
   int npend = 0;
   double pendCF[2] = {0.0, 0.0};
   // kinetic energy of deferred kicks with energies (mixed precision, free atoms): a
-  // boost that needs new forces sets keMode, and the pair launch then also sums 2KE of
-  // P + keCF F and of P + 2 keCF F (the momenta after the next identical half-kick
-  // of a velocity-Verlet loop, kept as keSpec until P, F or the layer change) and
-  // sets keDone
-  int keMode = 0;
-  double keCF = 0.0;
-  bool keDone = false;
-  float2* dKEPair = nullptr;   // per tile: 6 float-float partials of those sums
-  int kePairCap = 0;
+  // boost that needed new forces also sums 2KE of P + 2 CF F, the momenta after the
+  // next identical half-kick of a velocity-Verlet loop, kept as keSpec until P, F
+  // or the layer change
   bool keSpecValid = false;
   double keSpecCF = 0.0, keSpec[3] = {0.0, 0.0, 0.0};
   bool skinReady = false, packReady = false;
