@@ -490,6 +490,268 @@ __global__ void __launch_bounds__(128) k_sg_mlp(TileArgs T, const float* __restr
     }
 }
 
+// ---- network: inference on the 5th-generation tensor cores (tcgen05) --------------
+//
+// The same computation as k_sg_mlp (BF16 operands rounded at the same points, FP32
+// accumulation) with tcgen05.mma: M = 128 atoms per tile (one species), operands in
+// shared memory in the canonical K-major layout without swizzle, accumulators in
+// tensor memory.  Persistent blocks of 128 threads hold the BF16 weights of both
+// species for their whole life and take 128-atom tiles in turn; thread t owns row t
+// of a tile, which is TMEM lane t (warp w reads lanes 32w..32w+31).  Thread 0
+// issues each GEMM (one tcgen05.mma per K = 16) and commits it to an mbarrier that
+// every thread waits on.  Per tile:
+//   Z1 = G W1          TMEM columns   0..63   (K = 32)
+//   A1 = silu(Z1 + b1) -> smem X,  Z2 = A1 W2               columns  64..127
+//   E = w3 . silu(Z2 + b2) + b3,  dZ2 = w3 silu'(Z2 + b2) -> X
+//   dA1 = dZ2 W2^T                                          columns 128..191
+//   dZ1 = dA1 silu'(Z1 + b1) -> X,  dE/dG = dZ1 W1^T        columns 192..223 (N = 32)
+// Waits are bounded: a wait that runs out sets *err, the block stops taking tiles,
+// frees its tensor memory and returns (the host reports the error).
+
+constexpr int TC_M = 128, TC_COLS = 256;
+
+// byte offset of element (r, k) of a K-major operand with K columns: 8 x 16-byte core
+// matrices, consecutive along K (leading byte offset 128), row groups of 8 K/8 core
+// matrices apart (stride byte offset 16 K)
+__host__ __device__ constexpr int tc_off(int r, int k, int K) {
+  return (r >> 3) * (K * 16) + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2;
+}
+
+struct TcWeights {   // one species, BF16 B operands (rows n, K contiguous) and FP32 vectors
+  alignas(128) unsigned char B1[64 * 32 * 2];   // Z1:  B1[n][k] = W1[k][n]   (N 64, K 32)
+  alignas(128) unsigned char B2[64 * 64 * 2];   // Z2:  B2[n][k] = W2[k][n]   (N 64, K 64)
+  alignas(128) unsigned char B3[64 * 64 * 2];   // dA1: B3[n][k] = W2[n][k]   (N 64, K 64)
+  alignas(128) unsigned char B4[32 * 64 * 2];   // dG:  B4[n][k] = W1[n][k]   (N 32, K 64)
+  float b1[H], b2[H], w3[H], b3;
+};
+
+struct TcSmem {
+  TcWeights w[NS];
+  alignas(128) unsigned char G[TC_M * DIN * 2];   // A operand of Z1 (K 32)
+  alignas(128) unsigned char X[TC_M * H * 2];     // A operand of the other GEMMs (K 64)
+  alignas(8) unsigned long long bar;
+  unsigned int taddr;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor: start address, leading and stride byte offsets,
+// descriptor version 1, no swizzle
+__device__ __forceinline__ unsigned long long tc_sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (unsigned long long)((addr >> 4) & 0x3FFFu) | ((unsigned long long)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((unsigned long long)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both K-major, M x N
+__host__ __device__ constexpr uint32_t tc_idesc(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// D[tmem] (+)= A[128 x K] B[K x N], issued by one thread, K / 16 instructions
+template <int K, int N>
+__device__ __forceinline__ void tc_gemm(uint32_t dtmem, const unsigned char* A, const unsigned char* B) {
+  const uint32_t a0 = smem_u32(A), b0 = smem_u32(B);
+  constexpr uint32_t idesc = tc_idesc(TC_M, N);
+#pragma unroll
+  for (int s = 0; s < K / 16; s++) {
+    const unsigned long long ad = tc_sdesc(a0 + 256u * s, 128u, 16u * K), bd = tc_sdesc(b0 + 256u * s, 128u, 16u * K);
+    const uint32_t acc = s > 0 ? 1u : 0u;
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
+        "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+  }
+}
+
+__device__ __forceinline__ void tc_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+               : "memory");
+}
+
+// bounded wait for the phase; false if it did not complete
+__device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t phase) {
+  for (int i = 0; i < (1 << 22); i++) {
+    uint32_t done;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(phase)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void proxy_fence() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// 16 consecutive FP32 columns of this thread's TMEM lane
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int q = 0; q < 16; q++) v[q] = __uint_as_float(r[q]);
+}
+
+// 8 BF16 values (from 8 floats) into one 16-byte chunk of a K-major operand
+__device__ __forceinline__ void tc_st8(unsigned char* base, int r, int k, int K, const float* v) {
+  uint4 w;
+  __nv_bfloat162 h[4];
+#pragma unroll
+  for (int q = 0; q < 4; q++) h[q] = __floats2bfloat162_rn(v[2 * q], v[2 * q + 1]);
+  memcpy(&w, h, 16);
+  *reinterpret_cast<uint4*>(base + tc_off(r, k, K)) = w;
+}
+
+__device__ void tc_load_weights(TcWeights& w, const float* p) {
+  for (int q = threadIdx.x; q < DIN * H; q += blockDim.x) {
+    const int k = q / H, n = q % H;   // W1[k][n]
+    const __nv_bfloat16 v = __float2bfloat16(p[OFF_W1 + q]);
+    *reinterpret_cast<__nv_bfloat16*>(w.B1 + tc_off(n, k, DIN)) = v;   // B1[n][k]
+    *reinterpret_cast<__nv_bfloat16*>(w.B4 + tc_off(k, n, H)) = v;     // B4[k][n] (rows: input index)
+  }
+  for (int q = threadIdx.x; q < H * H; q += blockDim.x) {
+    const int k = q / H, n = q % H;   // W2[k][n]
+    const __nv_bfloat16 v = __float2bfloat16(p[OFF_W2 + q]);
+    *reinterpret_cast<__nv_bfloat16*>(w.B2 + tc_off(n, k, H)) = v;   // B2[n][k]
+    *reinterpret_cast<__nv_bfloat16*>(w.B3 + tc_off(k, n, H)) = v;   // B3[k][n] (rows: a1 index)
+  }
+  for (int q = threadIdx.x; q < H; q += blockDim.x) {
+    w.b1[q] = p[OFF_B1 + q];
+    w.b2[q] = p[OFF_B2 + q];
+    w.w3[q] = p[OFF_W3 + q];
+  }
+  if (threadIdx.x == 0) w.b3 = p[OFF_B3];
+}
+
+__global__ void __launch_bounds__(128, 1) k_sg_mlp_tc(TileArgs T, const float* __restrict__ params,
+                                                      const float* __restrict__ Gin, float* __restrict__ Eatom,
+                                                      float* __restrict__ dEdG, int* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char raw[];
+  TcSmem& S = *reinterpret_cast<TcSmem*>(raw);
+  const int t = threadIdx.x, warp = t >> 5;
+  for (int sp = 0; sp < NS; sp++) tc_load_weights(S.w[sp], params + sp * PER_SPECIES);
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&S.taddr)),
+                 "r"(TC_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (t == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&S.bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  proxy_fence();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tm = S.taddr, bar = smem_u32(&S.bar);
+  const uint32_t lane_base = (uint32_t)(32 * warp) << 16;   // this warp's TMEM lanes
+  uint32_t phase = 0;
+  bool ok = true;
+  // one GEMM: operands written by all threads before, accumulator read by all after;
+  // ok stays block-uniform (every thread leaves the tile loop together)
+  auto run = [&](auto&& issue) {
+    proxy_fence();
+    tc_fence_before();
+    __syncthreads();
+    if (t == 0) {
+      tc_fence_after();
+      issue();
+      tc_commit(bar);
+    }
+    ok = __syncthreads_and(tc_wait(bar, phase) ? 1 : 0) != 0;
+    if (ok) phase ^= 1u;
+    tc_fence_after();
+  };
+  for (int ti = blockIdx.x; ti < T.ntiles; ti += gridDim.x) {
+    const int3 tile = T.tiles[ti];
+    const TcWeights& W = S.w[tile.z];
+    const bool have = t < tile.y;
+    const int atom = have ? T.atoms[tile.x + t] : 0;
+    {   // G row -> BF16 A operand
+      float g[DIN];
+#pragma unroll
+      for (int k = 0; k < DIN; k += 4) {
+        const float4 v = have ? *reinterpret_cast<const float4*>(Gin + (size_t)atom * DIN + k) : make_float4(0.f, 0.f, 0.f, 0.f);
+        g[k] = v.x;
+        g[k + 1] = v.y;
+        g[k + 2] = v.z;
+        g[k + 3] = v.w;
+      }
+#pragma unroll
+      for (int k = 0; k < DIN; k += 8) tc_st8(S.G, t, k, DIN, g + k);
+    }
+    run([&] { tc_gemm<DIN, H>(tm + 0, S.G, W.B1); });
+    if (!ok) break;
+#pragma unroll
+    for (int c = 0; c < H; c += 16) {   // A1 = silu(Z1 + b1)
+      float z[16];
+      tc_ld16(tm + lane_base + c, z);
+#pragma unroll
+      for (int q = 0; q < 16; q++) z[q] = silu(z[q] + W.b1[c + q]);
+      tc_st8(S.X, t, c, H, z);
+      tc_st8(S.X, t, c + 8, H, z + 8);
+    }
+    run([&] { tc_gemm<H, H>(tm + 64, S.X, W.B2); });
+    if (!ok) break;
+    float e = 0.f;
+#pragma unroll
+    for (int c = 0; c < H; c += 16) {   // E and dE/dZ2
+      float z[16];
+      tc_ld16(tm + lane_base + 64 + c, z);
+#pragma unroll
+      for (int q = 0; q < 16; q++) {
+        const float u = z[q] + W.b2[c + q];
+        e += W.w3[c + q] * silu(u);
+        z[q] = W.w3[c + q] * dsilu(u);
+      }
+      tc_st8(S.X, t, c, H, z);
+      tc_st8(S.X, t, c + 8, H, z + 8);
+    }
+    if (have) Eatom[atom] = e + W.b3;
+    run([&] { tc_gemm<H, H>(tm + 128, S.X, W.B3); });
+    if (!ok) break;
+#pragma unroll
+    for (int c = 0; c < H; c += 16) {   // dE/dZ1 = dE/dA1 silu'(Z1 + b1)
+      float d[16], z[16];
+      tc_ld16(tm + lane_base + 128 + c, d);
+      tc_ld16(tm + lane_base + c, z);
+#pragma unroll
+      for (int q = 0; q < 16; q++) d[q] *= dsilu(z[q] + W.b1[c + q]);
+      tc_st8(S.X, t, c, H, d);
+      tc_st8(S.X, t, c + 8, H, d + 8);
+    }
+    run([&] { tc_gemm<H, DIN>(tm + 192, S.X, W.B4); });
+    if (!ok) break;
+#pragma unroll
+    for (int c = 0; c < DIN; c += 16) {   // dE/dG
+      float d[16];
+      tc_ld16(tm + lane_base + 192 + c, d);
+      if (have)
+#pragma unroll
+        for (int q = 0; q < 16; q += 4)
+          *reinterpret_cast<float4*>(dEdG + (size_t)atom * DIN + c + q) = make_float4(d[q], d[q + 1], d[q + 2], d[q + 3]);
+    }
+  }
+  if (!ok && t == 0) {
+    atomicExch(err, 1);
+    tc_wait(bar, phase);   // the GEMM in flight, if it completes after all (bounded)
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tm), "r"(TC_COLS) : "memory");
+  }
+}
+
 // ---- network: training gradient -----------------------------------------------------
 //
 // Per atom: O_i = e_c(i) E_i - t_i,  t_i = dE_i/dG_i . u_i.  With z1 = G W1 + b1,
@@ -712,9 +974,11 @@ struct Surrogate {
   int total = 0, cap = 0;
   double L = 0, skin = 0;
   uint8_t* dSpecies = nullptr;
-  std::vector<int3> tiles;
+  std::vector<int3> tiles, tiles128;   // tiles of <= 64 and of <= 128 atoms of one species
   int* dAtoms = nullptr;
   int3* dTiles = nullptr;
+  int3* dTiles128 = nullptr;
+  int* dTcError = nullptr;
   float4* dPos = nullptr;
   int *dCellOf = nullptr, *dCounts = nullptr, *dStarts = nullptr, *dCursor = nullptr, *dSorted = nullptr;
   int *dList = nullptr, *dCount = nullptr, *dOverflow = nullptr;
@@ -742,10 +1006,22 @@ static void sg_build_lists(Surrogate& S, const double* dR, cudaStream_t st) {
   CK(cudaMemcpyAsync(S.dR0, dR, sizeof(double) * 3 * S.total, cudaMemcpyDeviceToDevice, st));
 }
 
+// Dynamic shared memory of k_sg_mlp_tc: at least 100 KB, so that at most two blocks
+// (2 x 256 tensor-memory columns of the SM's 512) share an SM.
+static size_t tc_smem_bytes() { return std::max(sizeof(sg::TcSmem) + 1024, (size_t)100 * 1024); }
+
+// The network: tcgen05 kernel (default) or the mma.sync one (EMDEE_SG_MMA=sync).
 static void sg_network(Surrogate& S, const float* dParams, cudaStream_t st) {
   using namespace sg;
-  TileArgs T{S.dAtoms, S.dTiles, (int)S.tiles.size()};
-  k_sg_mlp<<<T.ntiles, 128, sizeof(MlpSmem), st>>>(T, dParams, S.dG, S.dEatom, S.dEdG);
+  const char* e = getenv("EMDEE_SG_MMA");
+  if (e && !strcmp(e, "sync")) {
+    TileArgs T{S.dAtoms, S.dTiles, (int)S.tiles.size()};
+    k_sg_mlp<<<T.ntiles, 128, sizeof(MlpSmem), st>>>(T, dParams, S.dG, S.dEatom, S.dEdG);
+  } else {
+    TileArgs T{S.dAtoms, S.dTiles128, (int)S.tiles128.size()};
+    const int blocks = std::min(T.ntiles, 2 * 152);
+    k_sg_mlp_tc<<<blocks, 128, tc_smem_bytes(), st>>>(T, dParams, S.dG, S.dEatom, S.dEdG, S.dTcError);
+  }
   CK(cudaGetLastError());
 }
 
@@ -788,23 +1064,31 @@ void* EmDee_surrogate_create(int chains, int N, double L, const int* types, doub
   }
   CK(cudaMalloc(&S->dSpecies, N));
   CK(cudaMemcpy(S->dSpecies, sp.data(), N, cudaMemcpyHostToDevice));
-  // tiles of <= 64 atoms of one species, chain by chain
+  // tiles of <= 64 atoms of one species, chain by chain, and over the same atom
+  // list tiles of <= 128 (the tensor-memory kernel's M)
   std::vector<int> atoms;
   for (int c = 0; c < chains; c++)
     for (int s = 0; s < NS; s++) {
       std::vector<int> list;
       for (int i = 0; i < N; i++)
         if (sp[i] == s) list.push_back(c * N + i);
+      const int first = (int)atoms.size();
       for (size_t b = 0; b < list.size(); b += TILE) {
         const int cnt = (int)std::min<size_t>(TILE, list.size() - b);
         S->tiles.push_back(make_int3((int)atoms.size(), cnt, s));
         atoms.insert(atoms.end(), list.begin() + b, list.begin() + b + cnt);
       }
+      for (size_t b = 0; b < list.size(); b += TC_M)
+        S->tiles128.push_back(make_int3(first + (int)b, (int)std::min<size_t>(TC_M, list.size() - b), s));
     }
   CK(cudaMalloc(&S->dAtoms, sizeof(int) * atoms.size()));
   CK(cudaMemcpy(S->dAtoms, atoms.data(), sizeof(int) * atoms.size(), cudaMemcpyHostToDevice));
   CK(cudaMalloc(&S->dTiles, sizeof(int3) * S->tiles.size()));
   CK(cudaMemcpy(S->dTiles, S->tiles.data(), sizeof(int3) * S->tiles.size(), cudaMemcpyHostToDevice));
+  CK(cudaMalloc(&S->dTiles128, sizeof(int3) * S->tiles128.size()));
+  CK(cudaMemcpy(S->dTiles128, S->tiles128.data(), sizeof(int3) * S->tiles128.size(), cudaMemcpyHostToDevice));
+  CK(cudaMalloc(&S->dTcError, sizeof(int)));
+  CK(cudaMemset(S->dTcError, 0, sizeof(int)));
   const int cells = chains * G.M * G.M * G.M;
   const double rho = N / (L * L * L);
   S->cap = std::max(64, ((int)(2.0 * 4.18879 * std::pow(rc + skin, 3) * rho) + 31) / 32 * 32);
@@ -836,6 +1120,7 @@ void* EmDee_surrogate_create(int chains, int N, double L, const int* types, doub
   CK(cudaMalloc(&S->dPart, sizeof(float) * (size_t)S->trainBlocks * PER_SPECIES));
   CK(cudaMalloc(&S->dR0, sizeof(double) * 3 * T));
   CK(cudaFuncSetAttribute(k_sg_mlp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MlpSmem)));
+  CK(cudaFuncSetAttribute(k_sg_mlp_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes()));
   CK(cudaFuncSetAttribute(k_sg_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TrainSmem)));
   return S;
 }
@@ -878,9 +1163,13 @@ int EmDee_surrogate_forces(void* h, const double* dR, double* dF, double* dE, in
   if (dE) k_sg_chain_sum<<<S.G.chains, 256, 0, st>>>(S.dEatom, S.G.N, dE);
   int ov = 0;
   if (rebuild) {
-    CK(cudaMemcpyAsync(&ov, S.dOverflow, sizeof(int), cudaMemcpyDeviceToHost, st));
+    int flags[2];
+    CK(cudaMemcpyAsync(&flags[0], S.dOverflow, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&flags[1], S.dTcError, sizeof(int), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    ov = flags[0];
     if (ov > S.cap) fatal("surrogate forces", "a Verlet list outgrew its capacity");
+    if (flags[1]) fatal("surrogate forces", "a tensor-core GEMM of the network did not complete");
   }
   return ov;
 }
@@ -975,7 +1264,7 @@ void EmDee_surrogate_trajectory(void* h, double* dR, double* dP, double* dF, dou
 void EmDee_surrogate_destroy(void* h) {
   Surrogate* S = (Surrogate*)h;
   if (!S) return;
-  void* ptrs[] = {S->dSpecies, S->dAtoms, S->dTiles, S->dPos, S->dCellOf, S->dCounts, S->dStarts, S->dCursor,
+  void* ptrs[] = {S->dSpecies, S->dAtoms, S->dTiles, S->dTiles128, S->dTcError, S->dPos, S->dCellOf, S->dCounts, S->dStarts, S->dCursor,
                   S->dSorted, S->dList, S->dCount, S->dOverflow, S->dG, S->dU, S->dEdG, S->dEatom, S->dEres,
                   S->dV, S->dParams, S->dGrad, S->dM, S->dVar, S->dPart, S->dR0};
   for (void* p : ptrs) cudaFree(p);

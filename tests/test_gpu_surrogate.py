@@ -71,7 +71,49 @@ def test_descriptors(gpu, so, N):
     m.close()
 
 
-def test_network_energies_and_gradients(gpu, so):
+@pytest.fixture(params=["tcgen05", "mma.sync"])
+def engine(request):
+    """The network on the tcgen05 tensor cores (default) or on mma.sync."""
+    old = os.environ.get("EMDEE_SG_MMA")
+    if request.param == "mma.sync":
+        os.environ["EMDEE_SG_MMA"] = "sync"
+    else:
+        os.environ.pop("EMDEE_SG_MMA", None)
+    yield request.param
+    if old is None:
+        os.environ.pop("EMDEE_SG_MMA", None)
+    else:
+        os.environ["EMDEE_SG_MMA"] = old
+
+
+def test_network_engines_agree(gpu):
+    """tcgen05 (M = 128 tiles, TMEM accumulators) and mma.sync (64-atom tiles) round
+    the same BF16 operands; their FP32 sums differ only in order."""
+    N = 1728
+    R, L, types = config(N, 3, 12)
+    m = model(gpu, 3, N, L, types)
+    m.set_params(random_params(m.nparam, 13))
+    Rt = torch.tensor(R, device="cuda")
+    out = {}
+    for eng in ("sync", None):
+        if eng:
+            os.environ["EMDEE_SG_MMA"] = eng
+        else:
+            os.environ.pop("EMDEE_SG_MMA", None)
+        E, F = m.forces(Rt)
+        Ea, dG = m.atom_outputs()
+        out[eng] = (E.cpu(), F.cpu(), Ea.cpu(), dG.cpu())
+    os.environ.pop("EMDEE_SG_MMA", None)
+    a, b = out["sync"], out[None]
+    ea = (a[2] - b[2]).abs().max().item()
+    rg = ((a[3] - b[3]).norm() / a[3].norm()).item()
+    rf = ((a[1] - b[1]).norm() / a[1].norm()).item()
+    print("tcgen05 vs mma.sync: atom energies max %.2e, dE/dG rel %.2e, forces rel %.2e" % (ea, rg, rf))
+    assert ea < 2e-3 and rg < 5e-3 and rf < 5e-3
+    m.close()
+
+
+def test_network_energies_and_gradients(gpu, so, engine):
     N = 1728
     R, L, types = config(N, 2, 2)
     m = model(gpu, 2, N, L, types)
