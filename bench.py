@@ -384,6 +384,7 @@ def run_gpu(args):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32 pair math, f64 state",
                 "data": "synthetic (seeded fcc lattice, Maxwell-Boltzmann momenta)",
                 "config": workload_config(W, world=world), "neighbor_builds_in_timed_region": builds,
+                "tile_edge_cells": lib.EmDee_tile_edge(md),
                 "clocks": clk, "gpu_launches": int(launches), "roofline": roofline, "roofline_hbm": roofline_hbm,
                 "roofline_step": roofline_step,
                 "kernels": per_kernel, "e2e": e2e, "cpu_baseline": cpu, "workloads": extra}
@@ -397,10 +398,10 @@ def run_gpu(args):
 REPLICAS = dict(n=256, seed=86245, rc=2.5, skin=0.3, dt=0.005, nprop=100)
 
 
-def measure_replicas(lib, pkg, torch, steps):
+def measure_replicas(lib, pkg, torch, steps, count=None):
     rng = np.random.default_rng(REPLICAS["seed"])
     mds, sizes = [], []
-    for k in range(REPLICAS["n"]):
+    for k in range(REPLICAS["n"] if count is None else count):
         N = int(rng.integers(256, 8193))
         rho, T = float(rng.uniform(0.70, 0.90)), float(rng.uniform(0.8, 2.0))
         R, L = fcc(N, rho, 0.05, REPLICAS["seed"] + k)
@@ -425,6 +426,8 @@ def measure_replicas(lib, pkg, torch, steps):
     out = {"metric": METRIC, "value": total * steps / t, "unit": "atom-steps/s", "replicas": len(mds),
            "atoms": total, "N_min": min(sizes), "N_max": max(sizes), "steps": steps, "ms": 1e3 * t,
            "block_size": lib.lib.EmDee_replicas_block_size(b),
+           "pair_threads_per_atom": lib.lib.EmDee_replicas_pair_threads(b),
+           "tuning": "block size (256, 512, 1024) x pair threads per atom (1, 2), timed on copies of the batch",
            "neighbor_builds": sum(m.Builds for m in mds) - builds0,
            "timing": "host clock around one EmDee_replicas_run (one graph launch: a persistent kernel over all "
                      "replicas, then the results read back), device synchronized on both sides",
@@ -545,6 +548,39 @@ def measure_hmc(lib, torch, iterations, configs, epochs):
     return out
 
 
+def run_workload(args):
+    """One secondary workload alone, one JSON line (no headline fields): the replica
+    batch (--replicas boxes, --replica-steps steps) or repeated surrogate force
+    evaluations of --chains chains of the 8000-atom binary mixture."""
+    import torch
+    from emdee_gb300.build import build
+    build()
+    import emdee_gb300
+    lib = emdee_gb300.load()
+    if args.workload == "replicas":
+        out = measure_replicas(lib, emdee_gb300, torch, args.replica_steps, args.replicas)
+    else:
+        from emdee_gb300.surrogate import Chains, Surrogate
+        ch = Chains(lib, args.chains, 8000, 1000)
+        ch.run(20, 0.004, 20)
+        m = Surrogate(lib, args.chains, 8000, ch.L, ch.types)
+        m.init_params(3, -6.0)
+        R = ch.gather("R")
+        m.forces(R)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            E, F = m.forces(R, rebuild=False)
+        torch.cuda.synchronize()
+        t = time.perf_counter() - t0
+        out = {"workload": "surrogate forces", "chains": args.chains, "N": 8000, "evaluations": args.steps,
+               "ms_per_evaluation": 1e3 * t / args.steps,
+               "network": "tcgen05" if os.environ.get("EMDEE_SG_MMA") != "sync" else "mma.sync"}
+        m.close()
+        ch.close()
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -561,7 +597,14 @@ def main():
     ap.add_argument("--water-steps", type=int, default=500)
     ap.add_argument("--atoms", type=int, default=None,
                     help="smaller box of the same density (profiling runs); default 1,048,576")
+    ap.add_argument("--workload", default=None, choices=["replicas", "surrogate-forces"],
+                    help="run one secondary workload alone and print its measurement (profiling runs)")
+    ap.add_argument("--replicas", type=int, default=256, help="replica count of --workload replicas")
+    ap.add_argument("--chains", type=int, default=8, help="chains of --workload surrogate-forces")
     args = ap.parse_args()
+    if args.workload:
+        run_workload(args)
+        return
     if args.warmup < 3:
         args.warmup = 3
     if args.atoms:

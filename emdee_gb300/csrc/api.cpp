@@ -296,6 +296,10 @@ static void compute_forces_impl(tEmDee* md) {
   bool compute = md->Options.Compute;
   double t0 = wtime();
   flush_pending(s);   // deferred boosts use the forces they were issued with
+  if (!s.r0Valid && !s.tileTuned && s.precision == 0 && s.pairs_exist[s.layer - 1] && !two_level_active(s)) {
+    s.tileTuned = true;
+    device_tune_tile(s, pair_lj_only(s), [](System& sys) { device_pair_forces(sys, true); });
+  }
   bool rebuild = !s.r0Valid, forcesDone = false;
   if (!rebuild && s.skinReady && s.packReady && s.precision == 0 && s.pairs_exist[s.layer - 1]) {
     // the fused step left the skin decision and the packed positions on the device:
@@ -335,6 +339,7 @@ static void compute_forces_impl(tEmDee* md) {
     Elong = ewald_compute(s);
     Wlong = Ecoul + Elong - r[3];
   }
+  s.forcesF32 = s.precision == 0 && !s.coul[s.layer - 1].requires_kspace && s.bondedTerms.uploaded == 0;
   md->Virial.Total = r[2] + r[3] + Wlong + bonded[1] + bonded[3];
   md->Virial.Body = 0.0;
   if (s.nbodies != 0) {   // src/EmDeeData.f90:926-953
@@ -916,6 +921,7 @@ void EmDee_upload(tEmDee* md, char* option, double* address) {
     if (!s.initialized) fatal("upload", "box and coordinates have not been defined");
     CK(cudaMemcpyAsync(s.F(), address, sizeof(double) * n3, cudaMemcpyHostToDevice, s.stream));
     if (s.hMirrorF) memcpy(s.hMirrorF, address, sizeof(double) * n3);
+    s.forcesF32 = false;
   } else if (!strcmp(item, "charges")) {
     if (s.initialized) fatal("upload", "cannot set charges after box and coordinates initialization");
     for (int i = 0; i < s.natoms; i++) {
@@ -1083,6 +1089,7 @@ void EmDee_share_phase_space(tEmDee mdkeep, tEmDee* mdlose) {
 void EmDee_switch_model_layer(tEmDee* md, int layer) {
   System& s = *sys_of(*md);
   s.keSpecValid = false;
+  s.forcesF32 = false;
   flush_pending(s);   // pending kicks belong to the current layer's forces
   if (layer != s.layer) {
     if (layer < 1 || layer > s.nlayers) fatal("model layer switch", "selected layer is out of range");
@@ -1416,6 +1423,8 @@ void EmDee_pair_statistics(tEmDee md, long* listed, long* within) {
 }
 
 long EmDee_launch_count(tEmDee md) { return sys_of(md)->prof.total; }
+
+int EmDee_tile_edge(tEmDee md) { return sys_of(md)->grid.TB; }
 
 long EmDee_neighbor_pairs(tEmDee md, int* pairs, long capacity) {
   System& s = *sys_of(md);

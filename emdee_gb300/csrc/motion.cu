@@ -6,6 +6,7 @@
 // move:   R <- CR R + CP P/m (src/EmDeeData.f90:823-860).
 // FP64 throughout; compiled with -fmad=false so each update rounds exactly like
 // the reference's statement.
+#include "fpconv.h"
 #include "reduce.cuh"
 #include <vector>
 
@@ -270,6 +271,62 @@ __global__ void __launch_bounds__(MOTION_THREADS) k_kinetic_two(const double* __
   grid_reduce<6, MOTION_THREADS>(v, partials, ticket, result + 48, hostResult + 48);
 }
 
+// The same two sums with 2 FP64 operations per component instead of 4, for unit
+// masses and forces that are exact FP32 values (the mixed-precision pair forces):
+// p1 = P + CF F in FP64 exactly as the deferred kick will compute it, then p1 as a
+// float pair (hi + lo, 48 bits: integer rounding and one FP64 subtraction), and the
+// squares, the second kick and the sums in float-float arithmetic on the FP32 pipe
+// (error-free products by fused multiply-add, Knuth's two-sum).
+__device__ __forceinline__ float fp_round(double x) {   // round to nearest (normal floats; others 0)
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return d2f_normal(b) ? __uint_as_float(d2f_bits(b)) : 0.0f;
+}
+__device__ __forceinline__ double fp_exact(float f) {   // a normal float (or zero) as a double
+  const unsigned int u = __float_as_uint(f);
+  const unsigned int e = (u >> 23) & 255u;
+  if (e == 0) return 0.0;
+  return __longlong_as_double((long long)(((unsigned long long)(u & 0x80000000u) << 32) |
+                                          ((unsigned long long)(e + 896u) << 52) |
+                                          ((unsigned long long)(u & 0x7FFFFFu) << 29)));
+}
+__device__ __forceinline__ void ff_sq_acc(float h, float l, float& Ah, float& Al) {
+  const float sq = h * h;
+  float e = fmaf(h, h, -sq);
+  e = fmaf(2.f * h, l, e);
+  const float t = Ah + sq, bp = t - Ah, err = (Ah - (t - bp)) + (sq - bp);
+  Ah = t;
+  Al = Al + e + err;
+}
+
+__global__ void __launch_bounds__(MOTION_THREADS) k_kinetic_two_ff(const double* __restrict__ P,
+                                                                   const double* __restrict__ F, int N, double cf,
+                                                                   float cfh, float cfl, float2* partials,
+                                                                   unsigned int* ticket, double* result,
+                                                                   double* hostResult) {
+  const size_t n3 = 3 * (size_t)N, stride = (size_t)gridDim.x * blockDim.x;
+  const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  float a1h = 0.f, a1l = 0.f, a2h = 0.f, a2l = 0.f;
+  for (size_t j = g; j < n3; j += stride) {
+    const double f = F[j], p1 = fma(cf, f, P[j]);
+    const float ff = fp_round(f), h1 = fp_round(p1), l1 = fp_round(p1 - fp_exact(h1));
+    ff_sq_acc(h1, l1, a1h, a1l);
+    // p2 = p1 + cf f in float-float: cf f = q + qe exactly up to cfl's rounding
+    const float q = cfh * ff;
+    float qe = fmaf(cfh, ff, -q);
+    qe = fmaf(cfl, ff, qe);
+    const float t = h1 + q, bp = t - h1;
+    const float te = ((h1 - (t - bp)) + (q - bp)) + (l1 + qe);
+    const float h2 = t + te, l2 = te - (h2 - t);
+    ff_sq_acc(h2, l2, a2h, a2l);
+  }
+  const int d = (int)(g % 3);
+  float vh[6] = {d == 0 ? a1h : 0.f, d == 1 ? a1h : 0.f, d == 2 ? a1h : 0.f,
+                 d == 0 ? a2h : 0.f, d == 1 ? a2h : 0.f, d == 2 ? a2h : 0.f};
+  float vl[6] = {d == 0 ? a1l : 0.f, d == 1 ? a1l : 0.f, d == 2 ? a1l : 0.f,
+                 d == 0 ? a2l : 0.f, d == 1 ? a2l : 0.f, d == 2 ? a2l : 0.f};
+  grid_reduce_ff2<6, MOTION_THREADS>(vh, vl, partials, ticket, result + 48, hostResult + 48);
+}
+
 void device_kinetic_two(System& s, double CF) {
   const int N = s.natoms;
   const int blocks = std::min(3 * ((N + 3 * MOTION_THREADS - 1) / (3 * MOTION_THREADS)), 3 * 152);
@@ -279,8 +336,15 @@ void device_kinetic_two(System& s, double CF) {
     CK(cudaMalloc(&s.dKE, sizeof(double) * 3 * s.keCap));
   }
   prof_begin(s, PK_BOOST);
-  (s.unitMass ? k_kinetic_two<true> : k_kinetic_two<false>)<<<blocks, MOTION_THREADS, 0, s.stream>>>(
-      s.dP, s.F(), s.dInvMass, N, CF, s.dKE, s.dTicket + 1, s.dResult, s.hResult);
+  static const bool fp64Only = getenv("EMDEE_KE_FP64") != nullptr;   // tuning switch: the FP64 pass
+  if (s.unitMass && s.forcesF32 && !fp64Only) {
+    const float ch = (float)CF, cl = (float)(CF - (double)ch);
+    k_kinetic_two_ff<<<blocks, MOTION_THREADS, 0, s.stream>>>(s.dP, s.F(), N, CF, ch, cl, (float2*)s.dKE,
+                                                             s.dTicket + 1, s.dResult, s.hResult);
+  } else {
+    (s.unitMass ? k_kinetic_two<true> : k_kinetic_two<false>)<<<blocks, MOTION_THREADS, 0, s.stream>>>(
+        s.dP, s.F(), s.dInvMass, N, CF, s.dKE, s.dTicket + 1, s.dResult, s.hResult);
+  }
   CK(cudaGetLastError());
   prof_end(s, PK_BOOST);
   CK(cudaStreamSynchronize(s.stream));

@@ -683,13 +683,83 @@ static size_t build_smem(const Grid& g, int ntypes) {
          (size_t)ntypes * ntypes + 16;
 }
 
-static int choose_tile(int M, double perCell) {
+// Tile edge: EMDEE_TILE, else the system's tuned edge (tileOverride), else a rule on
+// the atoms per cell.
+static int rule_tile(int M, double perCell) {
+  const int tb = perCell <= 4.0 ? 4 : perCell <= 9.0 ? 3 : perCell <= 24.0 ? 2 : 1;
+  return std::min(tb, M);
+}
+
+static int choose_tile(const System& s, int M, double perCell) {
   if (const char* e = getenv("EMDEE_TILE")) {
     int tb = atoi(e);
     if (tb >= 1 && tb <= 6) return std::min(tb, M);
   }
-  int tb = perCell <= 4.0 ? 4 : perCell <= 9.0 ? 3 : perCell <= 24.0 ? 2 : 1;
-  return std::min(tb, M);
+  if (s.tileOverride > 0) return std::min(s.tileOverride, M);
+  return rule_tile(M, perCell);
+}
+
+// Tile edge tuned on the system itself at its first build (mixed precision, M > 5,
+// EMDEE_TILE unset): for each edge of 3..6 cells, one list build and two launches of
+// the pair kernel, timed with CUDA events; the cost of an edge is the pair time plus
+// a seventh of the build time (a rebuild every ~7 steps, typical of a liquid with the
+// reference's skin).  The rule's edge stays unless another is more than 5 % cheaper.
+// The choice is kept per (cells per edge, atoms per cell to 1/8, types, model
+// variant) for the process, so systems of the same shape use the same tiles and give
+// bit-identical results.
+static std::vector<std::pair<std::vector<long>, int>> g_tileTuned;
+
+void device_tune_tile(System& s, bool ljOnly, void (*pair)(System&)) {
+  if (getenv("EMDEE_TILE") || (getenv("EMDEE_AUTOTUNE") && !strcmp(getenv("EMDEE_AUTOTUNE"), "0"))) return;
+  const double L = *s.Lbox;
+  const int M = std::max((int)std::floor(NDIV * L / s.xRc), 2 * NDIV + 1);
+  if (M <= 2 * NDIV + 1) return;
+  const double perCell = (double)s.natoms / ((double)M * M * M);
+  const std::vector<long> key = {M, (long)std::lround(perCell * 8.0), s.ntypes, ljOnly ? 1 : 0, s.nbodies > 0,
+                                 s.hasExclusions ? 1 : 0};
+  for (const auto& e : g_tileTuned)
+    if (e.first == key) {
+      s.tileOverride = e.second;
+      return;
+    }
+  const int rule = rule_tile(M, perCell);
+  cudaEvent_t e0, e1, e2;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaEventCreate(&e2));
+  double best = 1e30, ruleCost = 1e30;
+  int bestTB = rule;
+  for (int tb = 3; tb <= std::min(6, M); tb++) {
+    s.tileOverride = tb;
+    CK(cudaEventRecord(e0, s.stream));
+    device_build_lists(s);
+    CK(cudaEventRecord(e1, s.stream));
+    if (s.grid.TB != tb) continue;   // did not fit (halo or shared memory): the build shrank the edge
+    pair(s);
+    CK(cudaEventRecord(e2, s.stream));   // the first pair launch warms up; time the second
+    pair(s);
+    cudaEvent_t e3;
+    CK(cudaEventCreate(&e3));
+    CK(cudaEventRecord(e3, s.stream));
+    CK(cudaEventSynchronize(e3));
+    float msBuild = 0.f, msPair = 0.f;
+    CK(cudaEventElapsedTime(&msBuild, e0, e1));
+    CK(cudaEventElapsedTime(&msPair, e2, e3));
+    CK(cudaEventDestroy(e3));
+    const double cost = msPair + msBuild / 7.0;
+    if (tb == rule) ruleCost = cost;
+    if (cost < best) {
+      best = cost;
+      bestTB = tb;
+    }
+  }
+  if (ruleCost < 1e30 && best > 0.95 * ruleCost) bestTB = rule;
+  CK(cudaEventDestroy(e0));
+  CK(cudaEventDestroy(e1));
+  CK(cudaEventDestroy(e2));
+  s.tileOverride = bestTB;
+  s.r0Valid = false;   // the system's own first build comes next, with the chosen edge
+  g_tileTuned.push_back({key, bestTB});
 }
 
 // src/neighbor_lists.f90:175-195 (build part) and 199-300.  reuse: keep the tile
@@ -710,7 +780,7 @@ static bool build_lists(System& s, bool reuse) {
   int M = (int)std::floor(NDIV * L / xRc);
   M = std::max(M, 2 * NDIV + 1);
   double perCell = (double)N / ((double)M * M * M);
-  int TB = choose_tile(M, perCell);
+  int TB = choose_tile(s, M, perCell);
   reuse = reuse && g.M == M && g.TB == TB && g.maxHalo > 0 && g.tileStride > 0 && c.atoms >= (size_t)N;
   size_t smemLimit = 200 * 1024;
   for (;;) {

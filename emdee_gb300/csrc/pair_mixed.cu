@@ -154,8 +154,16 @@ __global__ void PAIR_BOUNDS k_pair_mixed(PairArgsF A) {
     uint16_t* myIn = REFILTER ? A.nbIn + ((size_t)t * (A.capIn >> 3) * A.tileStride + li) * 8 : nullptr;
     const int ai = REFILTER ? A.orig[si] : 0;
     uint4 cur = sub < nch ? __ldcs(lp + (size_t)sub * A.tileStride) : make_uint4(0u, 0u, 0u, 0u);
+#ifdef PAIR_PREFETCH2   // tuning define: list chunks requested two ahead of use
+    uint4 nx1 = sub + tpa < nch ? __ldcs(lp + (size_t)(sub + tpa) * A.tileStride) : cur;
+#endif
     for (int c = sub; c < nch; c += tpa) {
+#ifdef PAIR_PREFETCH2
+      const uint4 nxt = nx1;
+      nx1 = (c + 2 * tpa < nch) ? __ldcs(lp + (size_t)(c + 2 * tpa) * A.tileStride) : nx1;
+#else
       const uint4 nxt = (c + tpa < nch) ? __ldcs(lp + (size_t)(c + tpa) * A.tileStride) : cur;
+#endif
       const unsigned w[4] = {cur.x, cur.y, cur.z, cur.w};
       if (PACKED) {
         // entries 2k (low half of word k) and 2k + 1 (high half) side by side;

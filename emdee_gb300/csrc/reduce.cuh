@@ -144,6 +144,60 @@ __device__ __forceinline__ void warp_sum_ff(float (&hi)[NQ], float (&lo)[NQ]) {
     }
 }
 
+// Per-thread float-float values (hi + lo) -> result[q] (FP64), also into result2 if
+// set; partials holds NQ float2 per block.  Every level runs on the FP32 pipe.
+template <int NQ, int THREADS>
+__device__ __forceinline__ void grid_reduce_ff2(const float (&vh)[NQ], const float (&vl)[NQ], float2* partials,
+                                                unsigned int* ticket, double* result, double* result2) {
+  __shared__ float2 red2[NQ][THREADS / 32];
+  __shared__ bool last2;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  float hi[NQ], lo[NQ];
+#pragma unroll
+  for (int q = 0; q < NQ; q++) {
+    hi[q] = vh[q];
+    lo[q] = vl[q];
+  }
+  warp_sum_ff<NQ>(hi, lo);
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < NQ; q++) red2[q][warp] = make_float2(hi[q], lo[q]);
+  __syncthreads();
+  if (threadIdx.x < NQ) {
+    const int q = threadIdx.x;
+    float h = 0.f, l = 0.f;
+    for (int w = 0; w < nw; w++) ff_add(h, l, red2[q][w].x, red2[q][w].y);
+    partials[(size_t)blockIdx.x * NQ + q] = make_float2(h, l);
+    __threadfence();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) last2 = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last2) return;
+  __threadfence();
+#pragma unroll
+  for (int q = 0; q < NQ; q++) hi[q] = lo[q] = 0.f;
+  for (unsigned int b = threadIdx.x; b < gridDim.x; b += blockDim.x)   // block order per thread
+#pragma unroll
+    for (int q = 0; q < NQ; q++) {
+      const float2 x = __ldcg(&partials[(size_t)b * NQ + q]);
+      ff_add(hi[q], lo[q], x.x, x.y);
+    }
+  warp_sum_ff<NQ>(hi, lo);
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < NQ; q++) red2[q][warp] = make_float2(hi[q], lo[q]);
+  __syncthreads();
+  if (threadIdx.x < NQ) {
+    const int q = threadIdx.x;
+    float h = 0.f, l = 0.f;
+    for (int w = 0; w < nw; w++) ff_add(h, l, red2[q][w].x, red2[q][w].y);
+    result[q] = (double)h + (double)l;
+    if (result2) result2[q] = (double)h + (double)l;
+  }
+  if (threadIdx.x == 0) *ticket = 0;
+}
+
 // Per-thread FP32 values -> result[q] (FP64), also into result2 if set.  partials holds
 // NQ float2 per block.
 // The last block (ticket) sums the partials in block order; the result does not

@@ -207,7 +207,9 @@ __device__ void rep_build(RepShared& S, const double* Rb, float4* pos, int* cell
 // every type pair lj_cut without modifier, with the Lennard-Jones arithmetic in cell
 // units (E = 4 eps sr6 (sr6 - 1), W = 24 eps sr6 (2 sr6 - 1)); otherwise the
 // general model code.  COMPUTE: energies too (the virial is always summed).
-template <bool LJ, bool COMPUTE>
+// TPA threads per atom (1 or 2): with 2, the two threads of a pair take alternate
+// 4-entry chunks of the atom's list and add their partial forces at the end.
+template <bool LJ, bool COMPUTE, int TPA>
 __device__ __forceinline__ void rep_pairs(const RepDesc& D, const float4* pos, const float4* offTab,
                                           const NBParams<float>* ptab, const uint8_t* stype, float& Ep, float& Wp) {
   const NBParams<float> mdl = D.model.model;
@@ -220,16 +222,18 @@ __device__ __forceinline__ void rep_pairs(const RepDesc& D, const float4* pos, c
   const int* __restrict__ count = D.count;
   const int* __restrict__ orig = D.orig;
   double* __restrict__ F = D.F;
-  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+  const int sub = TPA == 1 ? 0 : (int)(threadIdx.x & (TPA - 1));
+  const unsigned pmask = TPA == 1 ? 0xffffffffu : (3u << ((threadIdx.x & 31) & ~1u));
+  for (int i = threadIdx.x / TPA; i < N; i += blockDim.x / TPA) {
     const float4 pi = pos[i];
     const int n = min(count[i], cap);
     const NBParams<float>* row = ptab + (nt > 1 ? stype[i] * nt : 0);
     float fx = 0.f, fy = 0.f, fz = 0.f;
     const int nch = (n + 3) >> 2;
     // 4 entries per 16-byte load, the next chunk requested before this one is used
-    uint4 cur = nch > 0 ? __ldg(&list[i]) : make_uint4(0u, 0u, 0u, 0u);
-    for (int c = 0; c < nch; c++) {
-      const uint4 nxt = c + 1 < nch ? __ldg(&list[(size_t)(c + 1) * N + i]) : cur;
+    uint4 cur = sub < nch ? __ldg(&list[(size_t)sub * N + i]) : make_uint4(0u, 0u, 0u, 0u);
+    for (int c = sub; c < nch; c += TPA) {
+      const uint4 nxt = c + TPA < nch ? __ldg(&list[(size_t)(c + TPA) * N + i]) : cur;
       const uint32_t w[4] = {cur.x, cur.y, cur.z, cur.w};
 #pragma unroll
       for (int u = 0; u < 4; u++) {
@@ -276,14 +280,21 @@ __device__ __forceinline__ void rep_pairs(const RepDesc& D, const float4* pos, c
       }
       cur = nxt;
     }
-    const int a = orig[i];
-    F[3 * a] = f2d_exact(fx * invw);
-    F[3 * a + 1] = f2d_exact(fy * invw);
-    F[3 * a + 2] = f2d_exact(fz * invw);
+    if (TPA == 2) {
+      fx += __shfl_xor_sync(pmask, fx, 1);
+      fy += __shfl_xor_sync(pmask, fy, 1);
+      fz += __shfl_xor_sync(pmask, fz, 1);
+    }
+    if (sub == 0) {
+      const int a = orig[i];
+      F[3 * a] = f2d_exact(fx * invw);
+      F[3 * a + 1] = f2d_exact(fy * invw);
+      F[3 * a + 2] = f2d_exact(fz * invw);
+    }
   }
 }
 
-template <int THREADS>
+template <int THREADS, int TPA>
 __global__ void __launch_bounds__(THREADS) k_replicas(const RepDesc* __restrict__ descs, const int* __restrict__ order,
                                                       int steps, double dt, int nprop, int Nmax, int cellsMax) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -374,10 +385,10 @@ __global__ void __launch_bounds__(THREADS) k_replicas(const RepDesc* __restrict_
     float Ep = 0.f, Wp = 0.f;
     const bool lj = D.ljAll != 0;
     if (lj) {
-      if (compute) rep_pairs<true, true>(D, pos, offTab, ptab, stype, Ep, Wp);
-      else rep_pairs<true, false>(D, pos, offTab, ptab, stype, Ep, Wp);
+      if (compute) rep_pairs<true, true, TPA>(D, pos, offTab, ptab, stype, Ep, Wp);
+      else rep_pairs<true, false, TPA>(D, pos, offTab, ptab, stype, Ep, Wp);
     } else {
-      rep_pairs<false, true>(D, pos, offTab, ptab, stype, Ep, Wp);
+      rep_pairs<false, true, TPA>(D, pos, offTab, ptab, stype, Ep, Wp);
     }
     {
       float hi[2] = {0.5f * Ep, 0.5f * Wp}, lo[2] = {0.f, 0.f};
@@ -436,7 +447,7 @@ struct Replicas {
   double* dOut = nullptr;
   double* hOut = nullptr;
   std::vector<void*> owned;
-  int n = 0, Nmax = 0, cellsMax = 0, threads = 0;
+  int n = 0, Nmax = 0, cellsMax = 0, threads = 0, tpa = 1;
   size_t smem = 0;
   cudaStream_t stream = nullptr;
   cudaGraphExec_t graph = nullptr;
@@ -447,30 +458,59 @@ struct Replicas {
   std::vector<tEmDee> savedMd;
 };
 
-static void rep_launch(Replicas& B, int steps, double dt, int nprop, cudaStream_t st) {
+template <int TPA>
+static void rep_launch_tpa(Replicas& B, int steps, double dt, int nprop, cudaStream_t st) {
   switch (B.threads) {
     case 256:
-      k_replicas<256><<<B.n, 256, B.smem, st>>>(B.dDesc, B.dOrder, steps, dt, nprop, B.Nmax, B.cellsMax);
+      k_replicas<256, TPA><<<B.n, 256, B.smem, st>>>(B.dDesc, B.dOrder, steps, dt, nprop, B.Nmax, B.cellsMax);
       break;
     case 512:
-      k_replicas<512><<<B.n, 512, B.smem, st>>>(B.dDesc, B.dOrder, steps, dt, nprop, B.Nmax, B.cellsMax);
+      k_replicas<512, TPA><<<B.n, 512, B.smem, st>>>(B.dDesc, B.dOrder, steps, dt, nprop, B.Nmax, B.cellsMax);
       break;
     default:
-      k_replicas<1024><<<B.n, 1024, B.smem, st>>>(B.dDesc, B.dOrder, steps, dt, nprop, B.Nmax, B.cellsMax);
+      k_replicas<1024, TPA><<<B.n, 1024, B.smem, st>>>(B.dDesc, B.dOrder, steps, dt, nprop, B.Nmax, B.cellsMax);
       break;
   }
+}
+
+static void rep_launch(Replicas& B, int steps, double dt, int nprop, cudaStream_t st) {
+  if (B.tpa == 2) rep_launch_tpa<2>(B, steps, dt, nprop, st);
+  else rep_launch_tpa<1>(B, steps, dt, nprop, st);
   CK(cudaGetLastError());
 }
 
 static void rep_set_smem(Replicas& B) {
-  CK(cudaFuncSetAttribute(k_replicas<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)B.smem));
-  CK(cudaFuncSetAttribute(k_replicas<512>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)B.smem));
-  CK(cudaFuncSetAttribute(k_replicas<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)B.smem));
+  const int b = (int)B.smem;
+  CK(cudaFuncSetAttribute(k_replicas<256, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+  CK(cudaFuncSetAttribute(k_replicas<512, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+  CK(cudaFuncSetAttribute(k_replicas<1024, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+  CK(cudaFuncSetAttribute(k_replicas<256, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+  CK(cudaFuncSetAttribute(k_replicas<512, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+  CK(cudaFuncSetAttribute(k_replicas<1024, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
 }
 
-// Chooses the block size by timing a few steps of every candidate on scratch
-// copies of the replicas' state (the systems themselves are not touched).
-static int rep_autotune(Replicas& B, double dt, int nprop) {
+// Chooses the block size and the pair phase's threads per atom by timing a few steps
+// of every candidate on scratch copies of the replicas' state (the systems themselves
+// are not touched).  The choice is kept per batch shape (the sorted replica sizes and
+// type counts) for the life of the process, so batches of the same shape run the same
+// configuration and give bit-identical results.
+static std::vector<std::pair<std::vector<int>, std::pair<int, int>>> g_repTuned;
+
+static std::vector<int> rep_shape(const Replicas& B) {
+  std::vector<int> key;
+  for (const RepDesc& d : B.desc) key.push_back(d.N * 16 + d.ntypes);
+  std::sort(key.begin(), key.end());
+  return key;
+}
+
+static void rep_autotune(Replicas& B, double dt, int nprop) {
+  const std::vector<int> key = rep_shape(B);
+  for (const auto& e : g_repTuned)
+    if (e.first == key) {
+      B.threads = e.second.first;
+      B.tpa = e.second.second;
+      return;
+    }
   std::vector<RepDesc> scratch = B.desc;
   std::vector<void*> tmp;
   for (int r = 0; r < B.n; r++) {
@@ -502,10 +542,12 @@ static int rep_autotune(Replicas& B, double dt, int nprop) {
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
-  int best = 1024;
+  int best = 1024, bestTpa = 1;
   float bestMs = 1e30f;
-  for (int th : {256, 512, 1024}) {
+  for (int cfg = 0; cfg < 6; cfg++) {
+    const int th = 256 << (cfg % 3), tpa = 1 + cfg / 3;
     B.threads = th;
+    B.tpa = tpa;
     rep_launch(B, 2, dt, nprop, B.stream);   // warm-up
     CK(cudaEventRecord(e0, B.stream));
     rep_launch(B, 10, dt, nprop, B.stream);
@@ -516,6 +558,7 @@ static int rep_autotune(Replicas& B, double dt, int nprop) {
     if (ms < bestMs) {
       bestMs = ms;
       best = th;
+      bestTpa = tpa;
     }
   }
   CK(cudaEventDestroy(e0));
@@ -523,7 +566,9 @@ static int rep_autotune(Replicas& B, double dt, int nprop) {
   B.dDesc = keep;
   CK(cudaFree(dScratch));
   for (void* p : tmp) CK(cudaFree(p));
-  return best;
+  B.threads = best;
+  B.tpa = bestTpa;
+  g_repTuned.push_back({key, {best, bestTpa}});
 }
 
 }  // namespace emdee
@@ -614,9 +659,12 @@ void* EmDee_replicas_create(int n, tEmDee** systems) {
   CK(cudaMalloc(&B->dOrder, sizeof(int) * n));
   CK(cudaMemcpy(B->dOrder, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
   rep_set_smem(*B);
+  // EMDEE_REPLICA_THREADS=threads[,pair threads per atom] fixes the configuration
   const char* e = getenv("EMDEE_REPLICA_THREADS");
   B->threads = e ? atoi(e) : 0;
   if (B->threads != 256 && B->threads != 512 && B->threads != 1024) B->threads = 0;
+  const char* comma = e ? strchr(e, ',') : nullptr;
+  B->tpa = comma && atoi(comma + 1) == 2 ? 2 : 1;
   return B;
 }
 
@@ -631,7 +679,7 @@ void EmDee_replicas_run(void* batch, int steps, double dt, int nprop) {
     s->keSpecValid = false;
     CK(cudaStreamSynchronize(s->stream));
   }
-  if (B.threads == 0) B.threads = rep_autotune(B, dt, nprop);
+  if (B.threads == 0) rep_autotune(B, dt, nprop);
   if (steps == 0) return;
   if (!B.graph || B.gSteps != steps || B.gDt != dt || B.gNprop != nprop) {
     if (B.graph) CK(cudaGraphExecDestroy(B.graph));
@@ -688,6 +736,8 @@ void EmDee_replicas_run(void* batch, int steps, double dt, int nprop) {
 }
 
 int EmDee_replicas_block_size(void* batch) { return ((Replicas*)batch)->threads; }
+
+int EmDee_replicas_pair_threads(void* batch) { return ((Replicas*)batch)->tpa; }
 
 // Forces, potential energy and virial of every replica at its current positions (lists
 // rebuilt from them, which then become the build positions R0); no step is taken and no

@@ -241,6 +241,9 @@ struct System {
   // next identical half-kick of a velocity-Verlet loop, kept as keSpec until P, F
   // or the layer change
   bool keSpecValid = false;
+  bool forcesF32 = false;
+  int tileOverride = 0;     // tile edge chosen by device_tune_tile (0: the rule)
+  bool tileTuned = false;   // the current layer's forces are exact FP32 values (mixed pair forces only)
   double keSpecCF = 0.0, keSpec[3] = {0.0, 0.0, 0.0};
   bool skinReady = false, packReady = false;
   bool phaseShared = false;   // R/P aliased with another system (no deferral then)
@@ -294,6 +297,9 @@ bool device_skin_check(System& s);
 // Cell binning, tile sort and neighbor-list build (src/neighbor_lists.f90:63-300).
 // With two-level lists active it builds the outer lists (radius rc + skin + outer skin).
 void device_build_lists(System& s);
+// Tile edge tuned by timing builds and pair launches on the system (first build, mixed
+// precision); pair(s) computes the forces once on the current lists.
+void device_tune_tile(System& s, bool ljOnly, void (*pair)(System&));
 // Two-level lists: the outer skin in effect for the system (0 = single-level lists),
 // and whether the next rebuild goes through them.
 double outer_delta(System& s);

@@ -261,6 +261,11 @@ interface
     type(tEmDee), value :: md
   end function EmDee_outer_builds
 
+  integer(c_int) function EmDee_tile_edge( md ) bind(C,name="EmDee_tile_edge")
+    import
+    type(tEmDee), value :: md
+  end function EmDee_tile_edge
+
   subroutine EmDee_destroy( md ) bind(C,name="EmDee_destroy")
     import
     type(tEmDee), intent(inout) :: md

@@ -255,6 +255,11 @@ void EmDee_pair_statistics(tEmDee md, long* listed, long* within);
 /* Number of CUDA kernels the library has launched for this system. */
 long EmDee_launch_count(tEmDee md);
 
+/* Edge, in cells, of the tiles the neighbor lists and force kernels work on: tuned
+   on the system's first build in mixed precision (timed list builds and force
+   launches; EMDEE_TILE fixes it, EMDEE_AUTOTUNE=0 keeps the rule of atoms per cell). */
+int EmDee_tile_edge(tEmDee md);
+
 /* No counterpart in the reference.  EmDee_boost's momentum update and
  * kinetic-energy sums on caller-owned device arrays, allocating nothing: for
  * callers that cannot call cudaMalloc at that point (when another allocator
@@ -283,12 +288,16 @@ void EmDee_destroy(tEmDee* md);
    boost(dt/2) with neighbor-list rebuilds on the skin check -- in one persistent
    kernel launch, with energies at every nprop-th step of the call, and
    writes Builds, Energy, Virial and Kinetic back into each tEmDee.  The first
-   run picks the block size by timing candidates on copies of the state; every
-   (steps, dt, nprop) combination is captured once in a CUDA graph.  Systems keep
+   run picks the block size and the pair phase's threads per atom by timing
+   candidates on copies of the state (kept per batch shape for the process;
+   EMDEE_REPLICA_THREADS=threads[,2] fixes them); every (steps, dt, nprop)
+   combination is captured once in a CUDA graph.  Systems keep
    their device arrays: they can be downloaded, or stepped alone, between runs. */
 void* EmDee_replicas_create(int n, tEmDee** systems);
 void EmDee_replicas_run(void* batch, int steps, double dt, int nprop);
 int EmDee_replicas_block_size(void* batch);
+/* Threads per atom (1 or 2) of the pair phase chosen with the block size. */
+int EmDee_replicas_pair_threads(void* batch);
 void EmDee_replicas_destroy(void* batch);
 /* Forces, potential energy and virial of every replica at its current positions (no step). */
 void EmDee_replicas_evaluate(void* batch);

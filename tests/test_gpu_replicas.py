@@ -60,6 +60,7 @@ def test_replicas_match_oracle_and_single_system(gpu, oracle):
     b, keep = batch(gpu, mds)
     gpu.lib.EmDee_replicas_run(b, STEPS, DT, NPROP)
     assert gpu.lib.EmDee_replicas_block_size(b) in (256, 512, 1024)
+    assert gpu.lib.EmDee_replicas_pair_threads(b) in (1, 2)
     for k, (N, rho, T) in enumerate(SPECS):
         got = state(gpu, mds[k], N)
         for lib, prec in ((oracle, None), (gpu, MIXED)):
