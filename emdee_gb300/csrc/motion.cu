@@ -277,14 +277,16 @@ __global__ void __launch_bounds__(MOTION_THREADS) k_kinetic_two(const double* __
 // float pair (hi + lo, 48 bits: integer rounding and one FP64 subtraction), and the
 // squares, the second kick and the sums in float-float arithmetic on the FP32 pipe
 // (error-free products by fused multiply-add, Knuth's two-sum).
-__device__ __forceinline__ float fp_round(double x) {   // round to nearest (normal floats; others 0)
+// round to nearest float: integer operations for results in the normal range, the
+// hardware conversion (on the FP64 pipe) for zero, tiny, huge, infinite and NaN values
+__device__ __forceinline__ float fp_round(double x) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  return d2f_normal(b) ? __uint_as_float(d2f_bits(b)) : 0.0f;
+  return d2f_normal(b) ? __uint_as_float(d2f_bits(b)) : (float)x;
 }
-__device__ __forceinline__ double fp_exact(float f) {   // a normal float (or zero) as a double
+__device__ __forceinline__ double fp_exact(float f) {   // a float as a double (exact)
   const unsigned int u = __float_as_uint(f);
   const unsigned int e = (u >> 23) & 255u;
-  if (e == 0) return 0.0;
+  if (e == 0 || e == 255u) return (double)f;
   return __longlong_as_double((long long)(((unsigned long long)(u & 0x80000000u) << 32) |
                                           ((unsigned long long)(e + 896u) << 52) |
                                           ((unsigned long long)(u & 0x7FFFFFu) << 29)));

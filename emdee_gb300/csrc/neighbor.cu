@@ -700,7 +700,8 @@ static int choose_tile(const System& s, int M, double perCell) {
 }
 
 // Tile edge tuned on the system itself at its first build (mixed precision, M > 5,
-// EMDEE_TILE unset): for each edge of 3..6 cells, one list build and two launches of
+// EMDEE_TILE unset): for each edge from min(rule - 1, 3) to 6 cells (the rule's edge
+// always among them), one list build and two launches of
 // the pair kernel, timed with CUDA events; the cost of an edge is the pair time plus
 // a seventh of the build time (a rebuild every ~7 steps, typical of a liquid with the
 // reference's skin).  The rule's edge stays unless another is more than 5 % cheaper.
@@ -729,7 +730,7 @@ void device_tune_tile(System& s, bool ljOnly, void (*pair)(System&)) {
   CK(cudaEventCreate(&e2));
   double best = 1e30, ruleCost = 1e30;
   int bestTB = rule;
-  for (int tb = 3; tb <= std::min(6, M); tb++) {
+  for (int tb = std::max(1, std::min(rule - 1, 3)); tb <= std::min(6, M); tb++) {
     s.tileOverride = tb;
     CK(cudaEventRecord(e0, s.stream));
     device_build_lists(s);

@@ -150,20 +150,15 @@ __global__ void PAIR_BOUNDS k_pair_mixed(PairArgsF A) {
     const int ti = VAR == 1 ? htype[qi] : 0;
     float fx = 0.f, fy = 0.f, fz = 0.f;
     f32x2 fx2 = 0ull, fy2 = 0ull, fz2 = 0ull, ep2 = 0ull, wp2 = 0ull;   // PACKED accumulators
+#ifdef PAIR_KAHAN
+    f32x2 ec2 = 0ull, wc2 = 0ull;   // compensations
+#endif
     int nIn = 0;
     uint16_t* myIn = REFILTER ? A.nbIn + ((size_t)t * (A.capIn >> 3) * A.tileStride + li) * 8 : nullptr;
     const int ai = REFILTER ? A.orig[si] : 0;
     uint4 cur = sub < nch ? __ldcs(lp + (size_t)sub * A.tileStride) : make_uint4(0u, 0u, 0u, 0u);
-#ifdef PAIR_PREFETCH2   // tuning define: list chunks requested two ahead of use
-    uint4 nx1 = sub + tpa < nch ? __ldcs(lp + (size_t)(sub + tpa) * A.tileStride) : cur;
-#endif
     for (int c = sub; c < nch; c += tpa) {
-#ifdef PAIR_PREFETCH2
-      const uint4 nxt = nx1;
-      nx1 = (c + 2 * tpa < nch) ? __ldcs(lp + (size_t)(c + 2 * tpa) * A.tileStride) : nx1;
-#else
       const uint4 nxt = (c + tpa < nch) ? __ldcs(lp + (size_t)(c + tpa) * A.tileStride) : cur;
-#endif
       const unsigned w[4] = {cur.x, cur.y, cur.z, cur.w};
       if (PACKED) {
         // entries 2k (low half of word k) and 2k + 1 (high half) side by side;
@@ -178,8 +173,22 @@ __global__ void PAIR_BOUNDS k_pair_mixed(PairArgsF A) {
           const f32x2 inv = pk2(r2.x < A.rc2 ? Ops<float>::rcp(r2.x) : 0.f, r2.y < A.rc2 ? Ops<float>::rcp(r2.y) : 0.f);
           const f32x2 sr2 = mul2(sigc2, inv), sr6 = mul2(mul2(sr2, sr2), sr2);
           const f32x2 W = mul2(sr6, fma2(eps48_2, sr6, meps24_2));
+#ifdef PAIR_KAHAN   // tuning define: per-thread compensated (Kahan) energy and virial sums
+          {
+            const f32x2 mone = pk2(-1.f, -1.f);
+            if (COMPUTE) {
+              const f32x2 y = fma2(mone, ec2, mul2(sr6, fma2(eps4_2, sr6, meps4_2))), t = add2(ep2, y);
+              ec2 = fma2(mone, y, fma2(mone, ep2, t));
+              ep2 = t;
+            }
+            const f32x2 y = fma2(mone, wc2, W), t = add2(wp2, y);
+            wc2 = fma2(mone, y, fma2(mone, wp2, t));
+            wp2 = t;
+          }
+#else
           if (COMPUTE) ep2 = fma2(sr6, fma2(eps4_2, sr6, meps4_2), ep2);
           wp2 = add2(wp2, W);
+#endif
           const f32x2 sc = mul2(W, inv);
           fx2 = fma2(sc, dx, fx2);
           fy2 = fma2(sc, dy, fy2);
@@ -253,8 +262,14 @@ __global__ void PAIR_BOUNDS k_pair_mixed(PairArgsF A) {
       fx = a.x + a.y;
       fy = b.x + b.y;
       fz = c.x + c.y;
+#ifdef PAIR_KAHAN
+      const float2 ce = up2(ec2), cw = up2(wc2);
+      if (COMPUTE) Ep += (ee.x - ce.x) + (ee.y - ce.y);
+      Wp += (ww.x - cw.x) + (ww.y - cw.y);
+#else
       if (COMPUTE) Ep += ee.x + ee.y;
       Wp += ww.x + ww.y;
+#endif
     }
     for (int o = tpa >> 1; o > 0; o >>= 1) {
       fx += __shfl_xor_sync(gmask, fx, o);
