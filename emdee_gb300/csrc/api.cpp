@@ -1426,6 +1426,12 @@ long EmDee_launch_count(tEmDee md) { return sys_of(md)->prof.total; }
 
 int EmDee_tile_edge(tEmDee md) { return sys_of(md)->grid.TB; }
 
+int EmDee_tile_threads(tEmDee md, int kernel) {
+  const System& s = *sys_of(md);
+  if (s.grid.tileStride <= 0) return 0;
+  return kernel == 0 ? build_block_threads(s) : pair_block_threads(s);
+}
+
 long EmDee_neighbor_pairs(tEmDee md, int* pairs, long capacity) {
   System& s = *sys_of(md);
   return device_neighbor_pairs(s, pairs, capacity);

@@ -271,25 +271,61 @@ __global__ void __launch_bounds__(MOTION_THREADS) k_kinetic_two(const double* __
   grid_reduce<6, MOTION_THREADS>(v, partials, ticket, result + 48, hostResult + 48);
 }
 
-// The same two sums with 2 FP64 operations per component instead of 4, for unit
-// masses and forces that are exact FP32 values (the mixed-precision pair forces):
-// p1 = P + CF F in FP64 exactly as the deferred kick will compute it, then p1 as a
-// float pair (hi + lo, 48 bits: integer rounding and one FP64 subtraction), and the
-// squares, the second kick and the sums in float-float arithmetic on the FP32 pipe
-// (error-free products by fused multiply-add, Knuth's two-sum).
-// round to nearest float: integer operations for results in the normal range, the
-// hardware conversion (on the FP64 pipe) for zero, tiny, huge, infinite and NaN values
+// The same two sums without FP64 arithmetic, for unit masses and forces that are
+// exact FP32 values (the mixed-precision pair forces): P split into a float pair
+// (hi + lo, 48 of its 53 bits) by integer operations, the kicks P + CF F and
+// P + 2 CF F, the squares and the sums in float-float arithmetic on the FP32 pipe
+// (error-free products by fused multiply-add, Knuth's two-sum).  Each term is
+// within ~2^-46 of its FP64 value, so the sums agree with the FP64 ones to
+// ~1e-14 (relative); the kernel is bound by its 48 bytes per atom of memory traffic.
+//
+// Values outside the ranges the integer paths cover (zero is covered; tiny, huge,
+// infinite and NaN values are not) take the hardware conversions in a separate
+// function, a branch the common path never takes.
+constexpr int KE_FF_LOADS = 4;
+__device__ __noinline__ float fp_round_slow(double x) { return (float)x; }
+__device__ __noinline__ void ff_split_slow(double x, float& hi, float& lo) {
+  hi = (float)x;
+  lo = (float)(x - (double)hi);
+}
+// round to nearest float
 __device__ __forceinline__ float fp_round(double x) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  return d2f_normal(b) ? __uint_as_float(d2f_bits(b)) : (float)x;
+  if (d2f_normal(b)) return __uint_as_float(d2f_bits(b));
+  if ((b << 1) == 0) return __uint_as_float((unsigned int)(b >> 32));   // +-0
+  return fp_round_slow(x);
 }
-__device__ __forceinline__ double fp_exact(float f) {   // a float as a double (exact)
-  const unsigned int u = __float_as_uint(f);
-  const unsigned int e = (u >> 23) & 255u;
-  if (e == 0 || e == 255u) return (double)f;
-  return __longlong_as_double((long long)(((unsigned long long)(u & 0x80000000u) << 32) |
-                                          ((unsigned long long)(e + 896u) << 52) |
-                                          ((unsigned long long)(u & 0x7FFFFFu) << 29)));
+// x = hi + lo with hi = RN(x) and lo = RN(x - hi); x - hi is exact: the mantissa
+// bits below the float's rounding point, an integer of at most 29 bits in units of
+// 2^(E - 1075) (E the biased FP64 exponent), converted to float with one rounding
+__device__ __forceinline__ void ff_split(double x, float& hi, float& lo) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int E = (int)((b >> 52) & 0x7FF);
+  const unsigned int sign = (unsigned int)(b >> 32) & 0x80000000u;
+  if (E < 949 || E > 1149) {   // hi or lo outside the normal float range
+    if ((b << 1) == 0) {
+      hi = lo = __uint_as_float(sign);
+      return;
+    }
+    ff_split_slow(x, hi, lo);
+    return;
+  }
+  const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
+  unsigned int r = ((unsigned int)(E - 896) << 23) | (unsigned int)(m >> 29);
+  const int rest = (int)(m & 0x1FFFFFFFu);
+  const bool up = rest > 0x10000000 || (rest == 0x10000000 && (r & 1u));
+  r += up ? 1u : 0u;
+  hi = __uint_as_float(sign | r);
+  const float scale = __uint_as_float((unsigned int)(E - 948) << 23);   // 2^(E - 1075)
+  const float l = (float)(up ? rest - 0x20000000 : rest) * scale;
+  lo = __uint_as_float(__float_as_uint(l) ^ sign);
+}
+// (h, l) = (ah + al) + (bh + bl), renormalised
+__device__ __forceinline__ void ff_add(float ah, float al, float bh, float bl, float& h, float& l) {
+  const float t = ah + bh, bp = t - ah;
+  const float te = ((ah - (t - bp)) + (bh - bp)) + (al + bl);
+  h = t + te;
+  l = te - (h - t);
 }
 __device__ __forceinline__ void ff_sq_acc(float h, float l, float& Ah, float& Al) {
   const float sq = h * h;
@@ -301,25 +337,37 @@ __device__ __forceinline__ void ff_sq_acc(float h, float l, float& Ah, float& Al
 }
 
 __global__ void __launch_bounds__(MOTION_THREADS) k_kinetic_two_ff(const double* __restrict__ P,
-                                                                   const double* __restrict__ F, int N, double cf,
-                                                                   float cfh, float cfl, float2* partials,
-                                                                   unsigned int* ticket, double* result,
-                                                                   double* hostResult) {
+                                                                   const double* __restrict__ F, int N, float cfh,
+                                                                   float cfl, float2* partials, unsigned int* ticket,
+                                                                   double* result, double* hostResult) {
   const size_t n3 = 3 * (size_t)N, stride = (size_t)gridDim.x * blockDim.x;
   const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   float a1h = 0.f, a1l = 0.f, a2h = 0.f, a2l = 0.f;
-  for (size_t j = g; j < n3; j += stride) {
-    const double f = F[j], p1 = fma(cf, f, P[j]);
-    const float ff = fp_round(f), h1 = fp_round(p1), l1 = fp_round(p1 - fp_exact(h1));
-    ff_sq_acc(h1, l1, a1h, a1l);
-    // p2 = p1 + cf f in float-float: cf f = q + qe exactly up to cfl's rounding
-    const float q = cfh * ff;
-    float qe = fmaf(cfh, ff, -q);
-    qe = fmaf(cfl, ff, qe);
-    const float t = h1 + q, bp = t - h1;
-    const float te = ((h1 - (t - bp)) + (q - bp)) + (l1 + qe);
-    const float h2 = t + te, l2 = te - (h2 - t);
-    ff_sq_acc(h2, l2, a2h, a2l);
+  // KE_FF_LOADS components per thread in flight (the stride is a multiple of 3, so
+  // every component of a thread has the same dimension)
+  for (size_t j0 = g; j0 < n3; j0 += KE_FF_LOADS * stride) {
+    double pv[KE_FF_LOADS], fv[KE_FF_LOADS];
+#pragma unroll
+    for (int u = 0; u < KE_FF_LOADS; u++) {
+      const size_t j = j0 + u * stride;
+      pv[u] = j < n3 ? P[j] : 0.0;
+      fv[u] = j < n3 ? F[j] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < KE_FF_LOADS; u++) {
+      if (j0 + u * stride >= n3) break;
+      float ph, pl;
+      ff_split(pv[u], ph, pl);
+      const float ff = fp_round(fv[u]);
+      // cf f = q + qe, exact up to cfl's rounding
+      const float q = cfh * ff;
+      const float qe = fmaf(cfl, ff, fmaf(cfh, ff, -q));
+      float h1, l1, h2, l2;
+      ff_add(ph, pl, q, qe, h1, l1);   // P + cf f
+      ff_sq_acc(h1, l1, a1h, a1l);
+      ff_add(h1, l1, q, qe, h2, l2);   // P + 2 cf f
+      ff_sq_acc(h2, l2, a2h, a2l);
+    }
   }
   const int d = (int)(g % 3);
   float vh[6] = {d == 0 ? a1h : 0.f, d == 1 ? a1h : 0.f, d == 2 ? a1h : 0.f,
@@ -332,16 +380,20 @@ __global__ void __launch_bounds__(MOTION_THREADS) k_kinetic_two_ff(const double*
 void device_kinetic_two(System& s, double CF) {
   const int N = s.natoms;
   const int blocks = std::min(3 * ((N + 3 * MOTION_THREADS - 1) / (3 * MOTION_THREADS)), 3 * 152);
-  if (s.keCap < 2 * blocks) {
+  // the float-float pass is latency-bound: as many blocks as fit at once (five per
+  // SM at its 47 registers, rounded down to a multiple of 3), each thread with
+  // KE_FF_LOADS loads in flight
+  const int ffBlocks = std::min(3 * ((N + 3 * MOTION_THREADS - 1) / (3 * MOTION_THREADS)), 5 * 152 / 3 * 3);
+  if (s.keCap < 2 * ffBlocks) {   // partials: 6 doubles (or float pairs) per block
     CK(cudaFree(s.dKE));
-    s.keCap = 2 * blocks;
+    s.keCap = 2 * ffBlocks;
     CK(cudaMalloc(&s.dKE, sizeof(double) * 3 * s.keCap));
   }
   prof_begin(s, PK_BOOST);
   static const bool fp64Only = getenv("EMDEE_KE_FP64") != nullptr;   // tuning switch: the FP64 pass
   if (s.unitMass && s.forcesF32 && !fp64Only) {
     const float ch = (float)CF, cl = (float)(CF - (double)ch);
-    k_kinetic_two_ff<<<blocks, MOTION_THREADS, 0, s.stream>>>(s.dP, s.F(), N, CF, ch, cl, (float2*)s.dKE,
+    k_kinetic_two_ff<<<ffBlocks, MOTION_THREADS, 0, s.stream>>>(s.dP, s.F(), N, ch, cl, (float2*)s.dKE,
                                                              s.dTicket + 1, s.dResult, s.hResult);
   } else {
     (s.unitMass ? k_kinetic_two<true> : k_kinetic_two<false>)<<<blocks, MOTION_THREADS, 0, s.stream>>>(

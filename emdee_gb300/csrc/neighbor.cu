@@ -453,7 +453,7 @@ struct BuildArgs {
   uint16_t* selfIdx;
   int cap, tileStride;
   int tpa, tpaShift;   // threads per atom of the split build (a power of 2) and its log2
-  int* layout;         // out: per tile off[0..haloCells] and cst[0..haloCells-1] (halo_layout_saved)
+  int* layout;         // out: per tile off[0..haloCells] and cst[0..haloCells-1] (stage_frame_saved)
   int* maxCount;
 };
 
@@ -467,7 +467,11 @@ __device__ __forceinline__ bool excluded(const BuildArgs& A, int a, int b) {
   return false;
 }
 
-static const int BUILD_THREADS = 256;         // upper bound; launches use one thread per tile atom
+// Blocks of the thread-per-atom build: at most BUILD_THREADS threads, each taking
+// the same number of the tile's atoms (tile_threads); without a tuned count, as few
+// rounds as blocks of BUILD_THREADS_RULE threads allow.
+static const int BUILD_THREADS = 512;
+static const int BUILD_THREADS_RULE = 256;
 static const int BUILD_THREADS_SPLIT = 1024;  // split build: several threads per tile atom
 
 // List layout: for tile t, chunk c (8 entries) and tile-local atom li, the
@@ -492,16 +496,32 @@ __global__ void BUILD_BOUNDS k_build(BuildArgs A) {
   __shared__ int ws[33];
   const TileGeom g = A.g;
   const int t = blockIdx.x, cells = g.TB * g.TB * g.TB;
+  // shared memory: the staged halo (and a sentinel entry), the halo cell offsets,
+  // then for the general variant the halo atoms' slots, the type filter and the
+  // halo atoms' types
   float4* hpos = (float4*)sraw;
-  int* hslot = (int*)(hpos + A.haloCap + 1);
-  int* off = hslot + A.haloCap + 1;
-  int* cst = off + g.haloCells + 1;
-  int* hxyz = cst + g.haloCells;
+  int* off = (int*)(hpos + A.haloCap + 1);
+  int* hslot = off + g.haloCells + 1;
   const bool single = !GENERAL || A.ntypes == 1;
-  uint8_t* sinter = (uint8_t*)(hxyz + g.haloCells);
+  uint8_t* sinter = (uint8_t*)(hslot + (GENERAL ? A.haloCap + 1 : 0));
   uint8_t* htype = sinter + A.ntypes * A.ntypes;
   for (int k = threadIdx.x; k < A.ntypes * A.ntypes; k += blockDim.x) sinter[k] = A.interact[k];
-  const int haloCount = halo_layout(g, t, A.tab, A.start, off, cst, hxyz, ws);
+  // the layout, saved for the force kernels until the next build: first slots
+  // straight to global memory, cell sizes scanned into off
+  int* lay = A.layout + (size_t)t * (2 * g.haloCells + 1);
+  {
+    const int2* tt = A.tab + (size_t)t * g.haloCells;
+    for (int h = threadIdx.x; h < g.haloCells; h += blockDim.x) {
+      const int r = tt[h].x, b = A.start[r];
+      lay[g.haloCells + 1 + h] = b;
+      off[h] = A.start[r + 1] - b;
+    }
+    __syncthreads();
+    const int total = block_exclusive_scan<8>(off, g.haloCells, ws);
+    if (threadIdx.x == 0) off[g.haloCells] = total;
+    __syncthreads();
+  }
+  const int haloCount = off[g.haloCells];
   {
     // sizes taken from the previous build: a tile or halo that outgrew them is
     // reported (the host re-sizes and builds again) before anything is staged
@@ -511,13 +531,25 @@ __global__ void BUILD_BOUNDS k_build(BuildArgs A) {
       return;
     }
   }
-  {   // the layout, saved for the force kernels until the next build
-    int* dst = A.layout + (size_t)t * (2 * g.haloCells + 1);
-    for (int h = threadIdx.x; h <= g.haloCells; h += blockDim.x) dst[h] = off[h];
-    for (int h = threadIdx.x; h < g.haloCells; h += blockDim.x) dst[g.haloCells + 1 + h] = cst[h];
-  }
-  stage_frame_flat(g, off, cst, hxyz, A.pos4, hpos, hslot, single ? (uint8_t*)nullptr : htype, A.type8);
+  for (int h = threadIdx.x; h <= g.haloCells; h += blockDim.x) lay[h] = off[h];
+  // every thread reads back only the first slots it wrote itself
+  for (int h = threadIdx.x; h < g.haloCells; h += blockDim.x)
+    mark_halo_cell(hpos, h, off[h], off[h + 1], lay[g.haloCells + 1 + h]);
   __syncthreads();
+  stage_marked(g, haloCount, A.pos4, hpos, GENERAL ? hslot : nullptr, single ? (uint8_t*)nullptr : htype, A.type8);
+  __syncthreads();
+  // slot of halo index q (the general variant keeps them; the band test of the
+  // plain one, rare, looks its cell up)
+  auto slot_of = [&](int q) {
+    if (GENERAL) return hslot[q];
+    int lo = 0, hi = g.haloCells - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (off[mid] <= q) lo = mid;
+      else hi = mid - 1;
+    }
+    return lay[g.haloCells + 1 + lo] + (q - off[lo]);
+  };
   const bool none = A.ntypes == 1 && !sinter[0];   // the only type pair does not interact: empty lists
   const bool filterByAtom = GENERAL && (A.hasBodies || A.hasEx);
   const bool layered = GENERAL && A.layered;
@@ -566,6 +598,10 @@ __global__ void BUILD_BOUNDS k_build(BuildArgs A) {
         const float w = rem * rsqrtf(rem) + 1e-3f;   // approximate square root: within the margin
         const float xlo = pi.x - w;
         xhi = pi.x + w;
+        // atoms of halo cells left of floor(xlo) lie at x <= floor(xlo) <= xlo (cell
+        // hx spans [hx - C, hx - C + 1] in the frame): start at that cell
+        const int cs = min(max((int)floorf(xlo) + g.C, hcx - 2), hcx + 2);
+        q = off[h0 + cs - (hcx - 2)];
         while (q < q1 && hpos[q].x <= xlo) q++;
       }
       // candidates in groups of CG: the loads and distance tests of a group are
@@ -598,7 +634,7 @@ __global__ void BUILD_BOUNDS k_build(BuildArgs A) {
           if (!((cand >> u) & 1u)) continue;
           const int qu = q + u;
           const float r2 = r2s[u];
-          if (!(r2 < A.lo2 || exact_inside(A.R, A.L, ai, A.orig[hslot[qu]], A.thr))) continue;
+          if (!(r2 < A.lo2 || exact_inside(A.R, A.L, ai, A.orig[slot_of(qu)], A.thr))) continue;
           if (GENERAL && !single && !sinter[ti * A.ntypes + htype[qu]]) continue;
           if (filterByAtom) {
             const int aj = A.orig[hslot[qu]];
@@ -607,7 +643,7 @@ __global__ void BUILD_BOUNDS k_build(BuildArgs A) {
           }
           bool inner = true;
           if (layered)
-            inner = r2 < A.loIn2 || (r2 < A.hiIn2 && exact_inside(A.R, A.L, ai, A.orig[hslot[qu]], A.thrIn));
+            inner = r2 < A.loIn2 || (r2 < A.hiIn2 && exact_inside(A.R, A.L, ai, A.orig[slot_of(qu)], A.thrIn));
           f(qu, inner);
         }
         if (last) break;
@@ -678,9 +714,18 @@ static void grow(T*& p, size_t& have, size_t need) {
 }
 
 
-static size_t build_smem(const Grid& g, int ntypes) {
-  return (size_t)(g.maxHalo + 1) * (sizeof(float4) + sizeof(int) + 1) + 3 * sizeof(int) * (g.haloCells + 1) +
-         (size_t)ntypes * ntypes + 16;
+int build_block_threads(const System& s) {
+  return tile_threads(s.grid.tileStride, s.buildRounds, s.buildRounds > 0 ? BUILD_THREADS : BUILD_THREADS_RULE);
+}
+
+// the general build variant: several types, bodies, exclusions or layered lists
+static bool build_general(const System& s) {
+  return s.ntypes > 1 || s.nbodies > 0 || s.hasExclusions || s.xInRcSq < s.xRcSq;
+}
+
+static size_t build_smem(const Grid& g, int ntypes, bool general) {
+  return (size_t)(g.maxHalo + 1) * (sizeof(float4) + (general ? sizeof(int) + 1 : 0)) +
+         sizeof(int) * (g.haloCells + 1) + (size_t)ntypes * ntypes + 16;
 }
 
 // Tile edge: EMDEE_TILE, else the system's tuned edge (tileOverride), else a rule on
@@ -699,16 +744,35 @@ static int choose_tile(const System& s, int M, double perCell) {
   return rule_tile(M, perCell);
 }
 
-// Tile edge tuned on the system itself at its first build (mixed precision, M > 5,
-// EMDEE_TILE unset): for each edge from min(rule - 1, 3) to 6 cells (the rule's edge
-// always among them), one list build and two launches of
-// the pair kernel, timed with CUDA events; the cost of an edge is the pair time plus
-// a seventh of the build time (a rebuild every ~7 steps, typical of a liquid with the
-// reference's skin).  The rule's edge stays unless another is more than 5 % cheaper.
-// The choice is kept per (cells per edge, atoms per cell to 1/8, types, model
-// variant) for the process, so systems of the same shape use the same tiles and give
+// Tile edge and block sizes tuned on the system itself at its first build (mixed
+// precision, M > 5, EMDEE_TILE unset).  For each edge from min(rule - 1, 3) to 6
+// cells (the rule's edge always among them) a first build sizes the tiles; then the
+// list build and the pair kernel (its second launch) are timed with CUDA events,
+// each after a pass that moves the memory traffic of an integration step, at the
+// rule's block size and at every block size that gives each thread the same
+// number of the tile's atoms (1 to 4 rounds, 64 to 512 threads).  The cost of an
+// edge is its fastest pair launch plus a seventh of its fastest build (a rebuild
+// every ~7 steps, typical of a liquid with the reference's skin).  The rule's edge
+// and block sizes stay unless another choice is more than 5 % cheaper.  The choice
+// is kept per (cells per edge, atoms per cell to 1/8, types, model variant) for the
+// process, so systems of the same shape use the same tiles and blocks and give
 // bit-identical results.
-static std::vector<std::pair<std::vector<long>, int>> g_tileTuned;
+// Reads and rewrites R and P with their own bits and reads F (zero is 0 at run
+// time): the memory traffic of an integration step, so that timed tuning launches
+// meet the L2 contents a step leaves.
+__global__ void k_touch(double* __restrict__ R, double* __restrict__ P, const double* __restrict__ F, long n,
+                        long long zero) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const long long f = __double_as_longlong(F[i]) & zero;
+    R[i] = __longlong_as_double(__double_as_longlong(R[i]) ^ f);
+    P[i] = __longlong_as_double(__double_as_longlong(P[i]) ^ f);
+  }
+}
+
+struct TileChoice {
+  int tb, buildRounds, pairRounds;
+};
+static std::vector<std::pair<std::vector<long>, TileChoice>> g_tileTuned;
 
 void device_tune_tile(System& s, bool ljOnly, void (*pair)(System&)) {
   if (getenv("EMDEE_TILE") || (getenv("EMDEE_AUTOTUNE") && !strcmp(getenv("EMDEE_AUTOTUNE"), "0"))) return;
@@ -720,47 +784,86 @@ void device_tune_tile(System& s, bool ljOnly, void (*pair)(System&)) {
                                  s.hasExclusions ? 1 : 0};
   for (const auto& e : g_tileTuned)
     if (e.first == key) {
-      s.tileOverride = e.second;
+      s.tileOverride = e.second.tb;
+      s.buildRounds = e.second.buildRounds;
+      s.pairRounds = e.second.pairRounds;
       return;
     }
   const int rule = rule_tile(M, perCell);
-  cudaEvent_t e0, e1, e2;
+  cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
-  CK(cudaEventCreate(&e2));
+  auto timed = [&](auto&& f) {
+    if (!s.phaseShared) {   // (shared R and P may belong to another system's stream)
+      k_touch<<<4 * 152, 256, 0, s.stream>>>(s.dR, s.dP, s.F(), 3L * s.natoms, 0LL);
+      CK(cudaGetLastError());
+      s.prof.total++;
+    }
+    CK(cudaEventRecord(e0, s.stream));
+    f();
+    CK(cudaEventRecord(e1, s.stream));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    return (double)ms;
+  };
   double best = 1e30, ruleCost = 1e30;
-  int bestTB = rule;
+  TileChoice choice = {rule, 0, 0};
   for (int tb = std::max(1, std::min(rule - 1, 3)); tb <= std::min(6, M); tb++) {
     s.tileOverride = tb;
-    CK(cudaEventRecord(e0, s.stream));
-    device_build_lists(s);
-    CK(cudaEventRecord(e1, s.stream));
+    s.buildRounds = s.pairRounds = 0;
+    device_build_lists(s);   // sizes the tiles of this edge
     if (s.grid.TB != tb) continue;   // did not fit (halo or shared memory): the build shrank the edge
-    pair(s);
-    CK(cudaEventRecord(e2, s.stream));   // the first pair launch warms up; time the second
-    pair(s);
-    cudaEvent_t e3;
-    CK(cudaEventCreate(&e3));
-    CK(cudaEventRecord(e3, s.stream));
-    CK(cudaEventSynchronize(e3));
-    float msBuild = 0.f, msPair = 0.f;
-    CK(cudaEventElapsedTime(&msBuild, e0, e1));
-    CK(cudaEventElapsedTime(&msPair, e2, e3));
-    CK(cudaEventDestroy(e3));
+    // rounds 0 (the rule) and the even splits with distinct block sizes
+    std::vector<int> rounds = {0}, sizes = {-1};
+    for (int r = 1; r <= 4; r++) {
+      const int th = tile_threads(s.grid.tileStride, r, 512);
+      if (th < 64 || (s.grid.tileStride + th - 1) / th != r) continue;
+      if (std::find(sizes.begin(), sizes.end(), th) != sizes.end()) continue;
+      rounds.push_back(r);
+      sizes.push_back(th);
+    }
+    double msBuild = 1e30, msPair = 1e30, ruleBuild = 0.0, rulePair = 0.0;
+    int rb = 0, rp = 0;
+    for (int r : rounds) {
+      s.buildRounds = r;
+      const double ms = timed([&] { device_build_lists(s); });
+      if (getenv("EMDEE_TUNE_LOG"))
+        fprintf(stderr, "  edge %d build, %d threads: %.1f us\n", tb, build_block_threads(s), 1e3 * ms);
+      if (r == 0) ruleBuild = ms;
+      if (ms < msBuild) {
+        msBuild = ms;
+        rb = r;
+      }
+    }
+    for (int r : rounds) {
+      s.pairRounds = r;
+      pair(s);   // warm-up
+      const double ms = timed([&] { pair(s); });
+      if (getenv("EMDEE_TUNE_LOG")) fprintf(stderr, "  edge %d pair, %d threads: %.1f us\n", tb, pair_block_threads(s), 1e3 * ms);
+      if (r == 0) rulePair = ms;
+      if (ms < msPair) {
+        msPair = ms;
+        rp = r;
+      }
+    }
     const double cost = msPair + msBuild / 7.0;
-    if (tb == rule) ruleCost = cost;
+    if (tb == rule) ruleCost = rulePair + ruleBuild / 7.0;
+    if (getenv("EMDEE_TUNE_LOG"))
+      fprintf(stderr, "tile edge %d (at most %d atoms per tile): cost %.1f us\n", tb, s.grid.tileStride, 1e3 * cost);
     if (cost < best) {
       best = cost;
-      bestTB = tb;
+      choice = {tb, rb, rp};
     }
   }
-  if (ruleCost < 1e30 && best > 0.95 * ruleCost) bestTB = rule;
+  if (ruleCost < 1e30 && best > 0.95 * ruleCost) choice = {rule, 0, 0};
   CK(cudaEventDestroy(e0));
   CK(cudaEventDestroy(e1));
-  CK(cudaEventDestroy(e2));
-  s.tileOverride = bestTB;
+  s.tileOverride = choice.tb;
+  s.buildRounds = choice.buildRounds;
+  s.pairRounds = choice.pairRounds;
   s.r0Valid = false;   // the system's own first build comes next, with the chosen edge
-  g_tileTuned.push_back({key, bestTB});
+  g_tileTuned.push_back({key, choice});
 }
 
 // src/neighbor_lists.f90:175-195 (build part) and 199-300.  reuse: keep the tile
@@ -851,7 +954,7 @@ static bool build_lists(System& s, bool reuse) {
     CK(cudaStreamSynchronize(s.stream));
     g.tileStride = std::max(32, (hmax[0] + 31) / 32 * 32);
     g.maxHalo = hmax[1];
-    size_t smem = build_smem(g, s.ntypes);
+    size_t smem = build_smem(g, s.ntypes, build_general(s));
     size_t smem64 = (size_t)(g.maxHalo + 1) * (4 * sizeof(double) + 1) + 2 * sizeof(int) * (g.haloCells + 1) + 64;
     if ((g.maxHalo > 65534 || smem > smemLimit || (s.precision == 1 && smem64 > smemLimit)) && TB > 1) {
       TB--;
@@ -925,8 +1028,8 @@ static bool build_lists(System& s, bool reuse) {
   A.maxCount = g.dTileInfo + 2 * g.nTiles + 2;
   grow(g.dLayout, g.layoutCap, (size_t)g.nTiles * (2 * g.haloCells + 1));
   A.layout = g.dLayout;
-  size_t smem = build_smem(g, s.ntypes);
-  const bool general = s.ntypes > 1 || A.hasBodies || A.hasEx || A.layered;
+  const bool general = build_general(s);
+  size_t smem = build_smem(g, s.ntypes, general);
   // Threads per atom: a system too small to fill the GPU with one thread per atom and
   // with long lists (more than 48 entries per thread) splits the stencil rows of each
   // atom over 2, 4 or 8 threads (blocks of up to 1024 threads).
@@ -947,7 +1050,7 @@ static bool build_lists(System& s, bool reuse) {
                   : (general ? (A.minimg ? k_build<true, true, false> : k_build<true, false, false>)
                              : (A.minimg ? k_build<false, true, false> : k_build<false, false, false>));
   const int buildThreads = std::max(halo_min_threads(geo), split ? std::min(BUILD_THREADS_SPLIT, g.tileStride * A.tpa)
-                                                                 : std::min(BUILD_THREADS, std::max(32, g.tileStride)));
+                                                                 : build_block_threads(s));
   CK(cudaFuncSetAttribute(kb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
 #ifdef EMDEE_MAX_CARVEOUT
   CK(cudaFuncSetAttribute(kb, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared));

@@ -21,7 +21,11 @@
 
 namespace emdee {
 
-static const int PAIR_THREADS = 256;   // upper bound; launches use one thread per tile atom
+// Blocks of the single-type variant: at most PAIR_THREADS threads, each taking the
+// same number of the tile's atoms (tile_threads); without a tuned count, as few
+// rounds as blocks of PAIR_THREADS_RULE threads allow.
+static const int PAIR_THREADS = 512;
+static const int PAIR_THREADS_RULE = 256;
 // The general variant (VAR 1) may run several threads per atom in blocks of up to
 // PAIR_THREADS_GENERAL threads.
 static const int PAIR_THREADS_GENERAL = 1024;
@@ -73,16 +77,9 @@ struct PairArgsF {
 };
 
 // FP64 distance test of the reference (src/neighbor_lists.f90:247-250) for halo
-// index q of the tile whose layout is off/cst: its halo cell is the last one that
-// starts at or before q.
-__device__ __noinline__ bool refilter_exact(const PairArgsF& A, const int* off, const int* cst, int ai, int q) {
-  int lo = 0, hi = A.g.haloCells - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (off[mid] <= q) lo = mid;
-    else hi = mid - 1;
-  }
-  return exact_inside(A.R, A.L, ai, A.orig[cst[lo] + (q - off[lo])], A.thrIn);
+// index q of the tile whose saved layout is lay.
+__device__ __noinline__ bool refilter_exact(const PairArgsF& A, const int* lay, int ai, int q) {
+  return exact_inside(A.R, A.L, ai, A.orig[saved_slot(A.g, lay, q)], A.thrIn);
 }
 
 // VAR 0: one atom type, Lennard-Jones with modifier MOD, no Coulomb term.
@@ -106,14 +103,12 @@ __global__ void PAIR_BOUNDS k_pair_mixed(PairArgsF A) {
   // every block would queue on the slow FP64 pipe)
   if (A.skip != nullptr && __double_as_longlong(*A.skip) != 0) return;
   extern __shared__ __align__(16) unsigned char sraw[];
-  __shared__ int ws[33];
   const TileGeom g = A.g;
   const int t = blockIdx.x, cells = g.TB * g.TB * g.TB;
+  // shared memory: the staged halo (and its sentinel), then the general variant's
+  // pair table and halo types; the layout stays in global memory
   float4* hpos = (float4*)sraw;
-  int* off = (int*)(hpos + A.haloCap + 1);
-  int* cst = off + g.haloCells + 1;
-  int* hxyz = cst + g.haloCells;
-  PairEntry<float>* tbl = (PairEntry<float>*)(hxyz + g.haloCells);
+  PairEntry<float>* tbl = (PairEntry<float>*)(hpos + A.haloCap + 1);
   const int ntab = VAR == 1 ? A.ntypes * A.ntypes : 0;
   uint8_t* htype = (uint8_t*)(tbl + ntab);
   for (int k = threadIdx.x; k < ntab; k += blockDim.x) tbl[k] = A.table[k];
@@ -121,8 +116,8 @@ __global__ void PAIR_BOUNDS k_pair_mixed(PairArgsF A) {
     hpos[A.haloCap] = make_float4(1e9f, 1e9f, 1e9f, 0.f);
     if (VAR == 1) htype[A.haloCap] = 0;
   }
-  halo_layout_saved(g, t, A.layout, off, cst, hxyz);
-  stage_frame_flat(g, off, cst, hxyz, A.pos4, hpos, (int*)nullptr, VAR == 1 ? htype : (uint8_t*)nullptr, A.type8);
+  const int* lay = A.layout + (size_t)t * (2 * g.haloCells + 1);
+  stage_frame_saved(g, lay, A.pos4, hpos, VAR == 1 ? htype : (uint8_t*)nullptr, A.type8);
   __syncthreads();
 
   NBParams<float> m0 = A.table[0].model;
@@ -209,7 +204,7 @@ __global__ void PAIR_BOUNDS k_pair_mixed(PairArgsF A) {
           dz -= A.Mf * rintf(dz / A.Mf);
         }
         const float r2 = dx * dx + dy * dy + dz * dz;
-        if (REFILTER && (r2 < A.lo2In || (r2 < A.hi2In && refilter_exact(A, off, cst, ai, qj)))) {
+        if (REFILTER && (r2 < A.lo2In || (r2 < A.hi2In && refilter_exact(A, lay, ai, qj)))) {
           if (nIn < A.capIn) myIn[(nIn >> 3) * (A.tileStride * 8) + (nIn & 7)] = (uint16_t)qj;
           nIn++;
         }
@@ -361,9 +356,13 @@ static size_t pair_args(System& s, bool useInRc, double rc2scaled, bool general,
   A.R = nullptr;
   A.L = L;
   A.innerMax = nullptr;
-  size_t smem = (size_t)(g.maxHalo + 1) * sizeof(float4) + sizeof(int) * (3 * g.haloCells + 1);
+  size_t smem = (size_t)(g.maxHalo + 1) * sizeof(float4);
   if (general) smem += sizeof(PairEntry<float>) * s.ntypes * s.ntypes + g.maxHalo + 17;
   return smem;
+}
+
+int pair_block_threads(const System& s) {
+  return tile_threads(s.grid.tileStride, s.pairRounds, s.pairRounds > 0 ? PAIR_THREADS : PAIR_THREADS_RULE);
 }
 
 // variant: 0 single-type Lennard-Jones without charges, 1 general, 2 pair count only
@@ -377,7 +376,8 @@ void device_pair_forces_mixed(System& s, bool compute, bool useInRc, double rc2s
   // (fewer than ~2048 threads per SM) and with long lists (more than 48 entries per
   // thread) split each list over 2, 4 or 8 threads of a warp (general variant only,
   // blocks of up to 1024 threads).  Threads per block: the tile's largest atom count
-  // times that, or fewer with several atoms per thread (EMDEE_PAIR_THREADS).
+  // times that, or fewer with several atoms per thread (EMDEE_PAIR_THREADS), the
+  // single-type variant in even rounds (pair_block_threads).
   const int maxTh = variant == 0 ? PAIR_THREADS : PAIR_THREADS_GENERAL;
   const double L3 = L * L * L, expected = s.natoms / L3 * 4.18879020478639 * s.xRcSq * s.xRc;
   int tpa = 1, shift = 0;
@@ -390,9 +390,9 @@ void device_pair_forces_mixed(System& s, bool compute, bool useInRc, double rc2s
   A.tpa = tpa;
   A.tpaShift = shift;
   static const int thEnv = getenv("EMDEE_PAIR_THREADS") ? atoi(getenv("EMDEE_PAIR_THREADS")) : 0;
-  const int th = std::max(halo_min_threads(A.g), thEnv >= 32 && thEnv % 32 == 0
-                                                     ? std::min(thEnv, maxTh)
-                                                     : std::min(maxTh, std::max(32, g.tileStride * tpa)));
+  const int th = std::max(halo_min_threads(A.g), thEnv >= 32 && thEnv % 32 == 0 ? std::min(thEnv, maxTh)
+                                                 : variant == 0 ? pair_block_threads(s)
+                                                                : std::min(maxTh, std::max(32, g.tileStride * tpa)));
   const int nt = g.nTiles;
   if (variant == 0) {
     const int mod = s.P(0, 0, s.layer - 1).model.p.modifier;
@@ -431,7 +431,7 @@ void device_pair_refilter(System& s, bool compute, const double* skip) {
   A.hi2In = (float)(A.thrIn * M2 * (1.0 + LIST_BAND));
   A.R = s.dR;
   A.innerMax = g.dTileInfo + 2 * g.nTiles + 4;
-  const int th = std::max(halo_min_threads(A.g), std::min(PAIR_THREADS, std::max(32, g.tileStride)));
+  const int th = std::max(halo_min_threads(A.g), tile_threads(g.tileStride, 0, PAIR_THREADS_RULE));
   const int mod = s.P(0, 0, s.layer - 1).model.p.modifier;
   if (compute) launch_lj<true, false, true>(s, A, smem, g.nTiles, th, mod);
   else launch_lj<false, false, true>(s, A, smem, g.nTiles, th, mod);

@@ -241,9 +241,12 @@ struct System {
   // next identical half-kick of a velocity-Verlet loop, kept as keSpec until P, F
   // or the layer change
   bool keSpecValid = false;
-  bool forcesF32 = false;
+  bool forcesF32 = false;   // the current layer's forces are exact FP32 values (mixed pair forces only)
   int tileOverride = 0;     // tile edge chosen by device_tune_tile (0: the rule)
-  bool tileTuned = false;   // the current layer's forces are exact FP32 values (mixed pair forces only)
+  // atoms per thread (rounds) of the list build and of the single-type pair kernel,
+  // chosen by device_tune_tile with the edge (0: the rule of tile_threads)
+  int buildRounds = 0, pairRounds = 0;
+  bool tileTuned = false;   // device_tune_tile has run for this system
   double keSpecCF = 0.0, keSpec[3] = {0.0, 0.0, 0.0};
   bool skinReady = false, packReady = false;
   bool phaseShared = false;   // R/P aliased with another system (no deferral then)
@@ -297,9 +300,13 @@ bool device_skin_check(System& s);
 // Cell binning, tile sort and neighbor-list build (src/neighbor_lists.f90:63-300).
 // With two-level lists active it builds the outer lists (radius rc + skin + outer skin).
 void device_build_lists(System& s);
-// Tile edge tuned by timing builds and pair launches on the system (first build, mixed
-// precision); pair(s) computes the forces once on the current lists.
+// Tile edge and block sizes tuned by timing builds and pair launches on the system
+// (first build, mixed precision); pair(s) computes the forces once on the current lists.
 void device_tune_tile(System& s, bool ljOnly, void (*pair)(System&));
+// Block sizes of the thread-per-atom list build and of the single-type mixed pair
+// kernel on the current lists.
+int build_block_threads(const System& s);
+int pair_block_threads(const System& s);
 // Two-level lists: the outer skin in effect for the system (0 = single-level lists),
 // and whether the next rebuild goes through them.
 double outer_delta(System& s);

@@ -121,6 +121,18 @@ __device__ int block_exclusive_scan(int* data, int n, int* warpSums) {
 // blocks with halo_min_threads.
 __host__ __device__ __forceinline__ int halo_min_threads(const TileGeom& g) { return (g.haloCells + 255) / 256 * 32; }
 
+// Threads of a block that owns a tile of up to `stride` atoms when each thread
+// takes `rounds` of them (rounds <= 0: as few rounds as `cap` threads allow): the
+// atoms spread evenly over the warps, so that no warp runs a last round alone
+// while the block holds its shared memory and registers.  A multiple of 32, at
+// most cap.
+__host__ __device__ __forceinline__ int tile_threads(int stride, int rounds, int cap) {
+  if (rounds <= 0) rounds = (stride + cap - 1) / cap;
+  int th = (stride + rounds - 1) / rounds;
+  th = (th + 31) / 32 * 32;
+  return th < 32 ? 32 : th > cap ? cap : th;
+}
+
 // off[h] = first halo index of halo cell h of tile t; off[haloCells] = halo size.
 __device__ __forceinline__ int halo_offsets(const TileGeom& g, int t, const int* start, int* off, int* ws) {
   for (int h = threadIdx.x; h < g.haloCells; h += blockDim.x) {
@@ -161,35 +173,21 @@ __device__ __forceinline__ int halo_layout(const TileGeom& g, int t, const int2*
   return total;
 }
 
-// Halo layout of tile t as written by the list build (layout: per tile
-// 2 haloCells + 1 ints: off[0..haloCells], then cst[0..haloCells-1]); hxyz from
-// the halo cell index.  Ends with a barrier.
-__device__ __forceinline__ int halo_layout_saved(const TileGeom& g, int t, const int* layout, int* off, int* cst,
-                                                 int* hxyz) {
-  const int* src = layout + (size_t)t * (2 * g.haloCells + 1);
-  for (int h = threadIdx.x; h <= g.haloCells; h += blockDim.x) off[h] = src[h];
-  for (int h = threadIdx.x; h < g.haloCells; h += blockDim.x) {
-    cst[h] = src[g.haloCells + 1 + h];
-    if (hxyz) hxyz[h] = (h % g.HW) | (((h / g.HW) % g.HW) << 8) | ((h / (g.HW * g.HW)) << 16);
-  }
-  __syncthreads();
-  return off[g.haloCells];
+// Halo staging in two passes that keep no layout in shared memory.  mark_halo_cell
+// (first pass, one thread per halo cell h with first halo index b, end e and first
+// slot s0) records for every halo index k its cell (x word of hpos[k]) and its slot
+// (y word); after a barrier, stage_marked loads the halo atoms 0..n-1 in the tile
+// frame, one thread per halo atom, U loads in flight per thread (a warp's loads
+// cover consecutive slots of cell runs); optionally records slots and types.
+// Ends without a barrier.
+__device__ __forceinline__ void mark_halo_cell(float4* hpos, int h, int b, int e, int s0) {
+  int2* mark = reinterpret_cast<int2*>(hpos);
+  for (int k = b; k < e; k++) mark[2 * k] = make_int2(h, s0 + k - b);
 }
 
-// Stages the halo of tile t in the tile frame with one thread per halo atom (the
-// loads of a warp cover consecutive slots of cell runs, several in flight per
-// thread).  A first pass records each halo index's cell in the x word of its
-// hpos entry, which the thread staging that entry then overwrites.  Needs the
-// layout in shared memory behind a barrier; ends without one.  Optionally
-// records slots and types.
-__device__ __forceinline__ void stage_frame_flat(const TileGeom& g, const int* off, const int* cst, const int* hxyz,
-                                                 const float4* pos4, float4* hpos, int* hslot, uint8_t* htype,
-                                                 const uint8_t* type8) {
-  int* hcell = reinterpret_cast<int*>(hpos);
-  for (int h = threadIdx.x; h < g.haloCells; h += blockDim.x)
-    for (int k = off[h], e = off[h + 1]; k < e; k++) hcell[4 * k] = h;
-  __syncthreads();
-  const int n = off[g.haloCells];
+__device__ __forceinline__ void stage_marked(const TileGeom& g, int n, const float4* pos4, float4* hpos, int* hslot,
+                                             uint8_t* htype, const uint8_t* type8) {
+  const int2* mark = reinterpret_cast<const int2*>(hpos);
   constexpr int U = 4;
   for (int k0 = threadIdx.x; k0 < n; k0 += U * blockDim.x) {
     float4 p[U];
@@ -198,25 +196,49 @@ __device__ __forceinline__ void stage_frame_flat(const TileGeom& g, const int* o
     for (int u = 0; u < U; u++) {
       const int k = k0 + u * blockDim.x;
       if (k < n) {
-        const int h = hcell[4 * k];
-        hh[u] = h;
-        slot[u] = cst[h] + k - off[h];
-        p[u] = pos4[slot[u]];
+        const int2 m = mark[2 * k];
+        hh[u] = m.x;
+        slot[u] = m.y;
+        p[u] = pos4[m.y];
       }
     }
 #pragma unroll
     for (int u = 0; u < U; u++) {
       const int k = k0 + u * blockDim.x;
       if (k < n) {
-        const int c = hxyz[hh[u]];
-        const float fx = (float)((c & 255) - g.C), fy = (float)(((c >> 8) & 255) - g.C),
-                    fz = (float)((c >> 16) - g.C);
+        const int h = hh[u], hy = h / g.HW;
+        const float fx = (float)(h - hy * g.HW - g.C), fy = (float)(hy % g.HW - g.C), fz = (float)(hy / g.HW - g.C);
         hpos[k] = make_float4(p[u].x + fx, p[u].y + fy, p[u].z + fz, p[u].w);
         if (hslot) hslot[k] = slot[u];
         if (htype) htype[k] = type8[slot[u]];
       }
     }
   }
+}
+
+// Stages the halo of tile t from the layout saved by the list build (global
+// memory: off[0..haloCells], then cst[0..haloCells-1]); returns the halo size.
+// Ends without a barrier.
+__device__ __forceinline__ int stage_frame_saved(const TileGeom& g, const int* __restrict__ lay, const float4* pos4,
+                                                 float4* hpos, uint8_t* htype, const uint8_t* type8) {
+  for (int h = threadIdx.x; h < g.haloCells; h += blockDim.x)
+    mark_halo_cell(hpos, h, lay[h], lay[h + 1], lay[g.haloCells + 1 + h]);
+  __syncthreads();
+  const int n = lay[g.haloCells];
+  stage_marked(g, n, pos4, hpos, nullptr, htype, type8);
+  return n;
+}
+
+// Slot of halo index q of the tile whose saved layout is lay: its halo cell is the
+// last one that starts at or before q.
+__device__ __forceinline__ int saved_slot(const TileGeom& g, const int* __restrict__ lay, int q) {
+  int lo = 0, hi = g.haloCells - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (lay[mid] <= q) lo = mid;
+    else hi = mid - 1;
+  }
+  return lay[g.haloCells + 1 + lo] + (q - lay[lo]);
 }
 
 // Exact float -> double conversion with integer operations (normal numbers and

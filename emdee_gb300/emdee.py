@@ -111,6 +111,7 @@ SIGNATURES = {
     "EmDee_pair_statistics": (None, [tEmDee, _P, _P]),
     "EmDee_launch_count": (C.c_long, [tEmDee]),
     "EmDee_tile_edge": (C.c_int, [tEmDee]),
+    "EmDee_tile_threads": (C.c_int, [tEmDee, C.c_int]),
     "EmDee_boost_noalloc": (C.c_int, [_P, _P, _P, _I, _D, _D, _P, _P]),
     "EmDee_replicas_create": (C.c_void_p, [_I, _P]),
     "EmDee_replicas_run": (None, [C.c_void_p, _I, _D, _I]),
@@ -139,7 +140,7 @@ SIGNATURES = {
 # entry points of the GB300 library with no counterpart in the reference
 EXTENSIONS = {"EmDee_set_precision", "EmDee_set_outer_skin", "EmDee_outer_builds", "EmDee_neighbor_pairs", "EmDee_destroy", "EmDee_cuda_stream",
               "EmDee_profile", "EmDee_kernel_times", "EmDee_pair_statistics",
-              "EmDee_launch_count", "EmDee_tile_edge", "EmDee_boost_noalloc", "EmDee_replicas_create", "EmDee_replicas_run",
+              "EmDee_launch_count", "EmDee_tile_edge", "EmDee_tile_threads", "EmDee_boost_noalloc", "EmDee_replicas_create", "EmDee_replicas_run",
               "EmDee_replicas_block_size", "EmDee_replicas_pair_threads", "EmDee_replicas_destroy", "EmDee_replicas_evaluate",
               "EmDee_replicas_checkpoint", "EmDee_replicas_restore", "EmDee_device_pointer",
               "EmDee_replicas_gather", "EmDee_replicas_scatter",

@@ -266,6 +266,12 @@ interface
     type(tEmDee), value :: md
   end function EmDee_tile_edge
 
+  integer(c_int) function EmDee_tile_threads( md, kernel ) bind(C,name="EmDee_tile_threads")
+    import
+    type(tEmDee), value :: md
+    integer(c_int), value :: kernel
+  end function EmDee_tile_threads
+
   subroutine EmDee_destroy( md ) bind(C,name="EmDee_destroy")
     import
     type(tEmDee), intent(inout) :: md

@@ -260,6 +260,11 @@ long EmDee_launch_count(tEmDee md);
    launches; EMDEE_TILE fixes it, EMDEE_AUTOTUNE=0 keeps the rule of atoms per cell). */
 int EmDee_tile_edge(tEmDee md);
 
+/* Threads per block of the thread-per-atom list build (kernel 0) and of the
+   single-type Lennard-Jones force kernel (kernel 1) on the current tiles: tuned with
+   the tile edge (every thread takes the same number of a tile's atoms). */
+int EmDee_tile_threads(tEmDee md, int kernel);
+
 /* No counterpart in the reference.  EmDee_boost's momentum update and
  * kinetic-energy sums on caller-owned device arrays, allocating nothing: for
  * callers that cannot call cudaMalloc at that point (when another allocator
