@@ -484,12 +484,15 @@ __device__ __forceinline__ size_t nb_index(int t, int capC, int tileStride, int 
 }
 
 // GENERAL: several atom types, bodies, exclusions or layered lists; MINIMG: M = 5.
-// BUILD_MIN_BLOCKS (compile-time): resident blocks per SM the register budget must allow
-#ifdef BUILD_MIN_BLOCKS
-#define BUILD_BOUNDS __launch_bounds__(SPLIT ? BUILD_THREADS_SPLIT : BUILD_THREADS, BUILD_MIN_BLOCKS)
-#else
-#define BUILD_BOUNDS __launch_bounds__(SPLIT ? BUILD_THREADS_SPLIT : BUILD_THREADS)
+// Register budget: the thread-per-atom variants get up to BUILD_MAXNREG registers
+// (blocks of at most BUILD_THREADS threads); the split variant, in blocks of up to
+// 1024 threads, 64.  Under launch bounds alone the compiler held this kernel at 64
+// registers with spills; 80 (71 used) gave the fastest builds on the 1M-atom
+// workload (745 vs 811 us per rebuild with the pair kernel at 72).
+#ifndef BUILD_MAXNREG
+#define BUILD_MAXNREG 80
 #endif
+#define BUILD_BOUNDS __maxnreg__(SPLIT ? 64 : BUILD_MAXNREG)
 template <bool GENERAL, bool MINIMG, bool SPLIT>
 __global__ void BUILD_BOUNDS k_build(BuildArgs A) {
   extern __shared__ __align__(16) unsigned char sraw[];

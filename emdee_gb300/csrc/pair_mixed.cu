@@ -30,12 +30,15 @@ static const int PAIR_THREADS_RULE = 256;
 // PAIR_THREADS_GENERAL threads.
 static const int PAIR_THREADS_GENERAL = 1024;
 #define PAIR_MAX_THREADS (VAR == 1 ? PAIR_THREADS_GENERAL : PAIR_THREADS)
-// PAIR_MIN_BLOCKS (compile-time): resident blocks per SM the register budget must allow
-#ifdef PAIR_MIN_BLOCKS   // single-type Lennard-Jones variant only
-#define PAIR_BOUNDS __launch_bounds__(PAIR_MAX_THREADS, (VAR == 0 && !REFILTER) ? PAIR_MIN_BLOCKS : 1)
-#else
-#define PAIR_BOUNDS __launch_bounds__(PAIR_MAX_THREADS)
+// Register budget: the single-type Lennard-Jones variant gets up to PAIR_MAXNREG
+// registers (blocks of at most PAIR_THREADS threads), the general variant, in blocks
+// of up to 1024 threads, 64, the filtering launches 128.  Under launch bounds alone
+// the compiler held the energy variant at 64; 72 measured fastest on the 1M-atom
+// workload (157 vs 165 us per launch; 68: 159 us, 80: 178 us).
+#ifndef PAIR_MAXNREG
+#define PAIR_MAXNREG 72
 #endif
+#define PAIR_BOUNDS __maxnreg__(VAR == 1 ? 64 : REFILTER ? 128 : PAIR_MAXNREG)
 
 struct PairArgsF {
   TileGeom g;
