@@ -36,7 +36,7 @@ UNITS = {
     "bonded.cu": ["-fmad=false"],
     "surrogate.cu": [],
 }
-HEADERS = ["system.hpp", "pairmath.cuh", "tile.cuh", "f32x2.cuh", "fpconv.h", "reduce.cuh", "rigid.cuh", "bodies.cuh", os.path.join("..", "..", "include", "emdee.h")]
+HEADERS = ["system.hpp", "pairmath.cuh", "tile.cuh", "f32x2.cuh", "ffkick.cuh", "fpconv.h", "reduce.cuh", "rigid.cuh", "bodies.cuh", os.path.join("..", "..", "include", "emdee.h")]
 
 
 def _stale(target, deps):

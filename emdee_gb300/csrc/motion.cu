@@ -6,6 +6,7 @@
 // move:   R <- CR R + CP P/m (src/EmDeeData.f90:823-860).
 // FP64 throughout; compiled with -fmad=false so each update rounds exactly like
 // the reference's statement.
+#include "ffkick.cuh"
 #include "fpconv.h"
 #include "reduce.cuh"
 #include <vector>
@@ -272,70 +273,9 @@ __global__ void __launch_bounds__(MOTION_THREADS) k_kinetic_two(const double* __
 }
 
 // The same two sums without FP64 arithmetic, for unit masses and forces that are
-// exact FP32 values (the mixed-precision pair forces): P split into a float pair
-// (hi + lo, 48 of its 53 bits) by integer operations, the kicks P + CF F and
-// P + 2 CF F, the squares and the sums in float-float arithmetic on the FP32 pipe
-// (error-free products by fused multiply-add, Knuth's two-sum).  Each term is
-// within ~2^-46 of its FP64 value, so the sums agree with the FP64 ones to
-// ~1e-14 (relative); the kernel is bound by its 48 bytes per atom of memory traffic.
-//
-// Values outside the ranges the integer paths cover (zero is covered; tiny, huge,
-// infinite and NaN values are not) take the hardware conversions in a separate
-// function, a branch the common path never takes.
+// exact FP32 values (the mixed-precision pair forces), in float-float arithmetic
+// (ffkick.cuh); the sums agree with the FP64 ones to ~1e-14 (relative).
 constexpr int KE_FF_LOADS = 4;
-__device__ __noinline__ float fp_round_slow(double x) { return (float)x; }
-__device__ __noinline__ void ff_split_slow(double x, float& hi, float& lo) {
-  hi = (float)x;
-  lo = (float)(x - (double)hi);
-}
-// round to nearest float
-__device__ __forceinline__ float fp_round(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  if (d2f_normal(b)) return __uint_as_float(d2f_bits(b));
-  if ((b << 1) == 0) return __uint_as_float((unsigned int)(b >> 32));   // +-0
-  return fp_round_slow(x);
-}
-// x = hi + lo with hi = RN(x) and lo = RN(x - hi); x - hi is exact: the mantissa
-// bits below the float's rounding point, an integer of at most 29 bits in units of
-// 2^(E - 1075) (E the biased FP64 exponent), converted to float with one rounding
-__device__ __forceinline__ void ff_split(double x, float& hi, float& lo) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const int E = (int)((b >> 52) & 0x7FF);
-  const unsigned int sign = (unsigned int)(b >> 32) & 0x80000000u;
-  if (E < 949 || E > 1149) {   // hi or lo outside the normal float range
-    if ((b << 1) == 0) {
-      hi = lo = __uint_as_float(sign);
-      return;
-    }
-    ff_split_slow(x, hi, lo);
-    return;
-  }
-  const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
-  unsigned int r = ((unsigned int)(E - 896) << 23) | (unsigned int)(m >> 29);
-  const int rest = (int)(m & 0x1FFFFFFFu);
-  const bool up = rest > 0x10000000 || (rest == 0x10000000 && (r & 1u));
-  r += up ? 1u : 0u;
-  hi = __uint_as_float(sign | r);
-  const float scale = __uint_as_float((unsigned int)(E - 948) << 23);   // 2^(E - 1075)
-  const float l = (float)(up ? rest - 0x20000000 : rest) * scale;
-  lo = __uint_as_float(__float_as_uint(l) ^ sign);
-}
-// (h, l) = (ah + al) + (bh + bl), renormalised
-__device__ __forceinline__ void ff_add(float ah, float al, float bh, float bl, float& h, float& l) {
-  const float t = ah + bh, bp = t - ah;
-  const float te = ((ah - (t - bp)) + (bh - bp)) + (al + bl);
-  h = t + te;
-  l = te - (h - t);
-}
-__device__ __forceinline__ void ff_sq_acc(float h, float l, float& Ah, float& Al) {
-  const float sq = h * h;
-  float e = fmaf(h, h, -sq);
-  e = fmaf(2.f * h, l, e);
-  const float t = Ah + sq, bp = t - Ah, err = (Ah - (t - bp)) + (sq - bp);
-  Ah = t;
-  Al = Al + e + err;
-}
-
 __global__ void __launch_bounds__(MOTION_THREADS) k_kinetic_two_ff(const double* __restrict__ P,
                                                                    const double* __restrict__ F, int N, float cfh,
                                                                    float cfl, float2* partials, unsigned int* ticket,
@@ -356,17 +296,7 @@ __global__ void __launch_bounds__(MOTION_THREADS) k_kinetic_two_ff(const double*
 #pragma unroll
     for (int u = 0; u < KE_FF_LOADS; u++) {
       if (j0 + u * stride >= n3) break;
-      float ph, pl;
-      ff_split(pv[u], ph, pl);
-      const float ff = fp_round(fv[u]);
-      // cf f = q + qe, exact up to cfl's rounding
-      const float q = cfh * ff;
-      const float qe = fmaf(cfl, ff, fmaf(cfh, ff, -q));
-      float h1, l1, h2, l2;
-      ff_add(ph, pl, q, qe, h1, l1);   // P + cf f
-      ff_sq_acc(h1, l1, a1h, a1l);
-      ff_add(h1, l1, q, qe, h2, l2);   // P + 2 cf f
-      ff_sq_acc(h2, l2, a2h, a2l);
+      ffk_two_kicks(pv[u], ffk_round(fv[u]), cfh, cfl, a1h, a1l, a2h, a2l);
     }
   }
   const int d = (int)(g % 3);

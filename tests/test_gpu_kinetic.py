@@ -3,10 +3,11 @@
 precision, where the kick itself is deferred into the next kernel that touches
 the momenta and only its kinetic energy is computed when the boost returns:
 
-* after a displacement, by the pair kernel that computes the new forces (which
-  also sums the kinetic energy of a second identical kick, used by the next
-  half-kick of a velocity-Verlet step when nothing changed in between);
-* otherwise by a kinetic-energy pass over P and F that writes nothing.
+* after a displacement, once the new forces are computed, by a pass over P and
+  F that writes nothing and also sums the kinetic energy of a second identical
+  kick, used by the next half-kick of a velocity-Verlet step when nothing
+  changed in between (float-float arithmetic for unit masses, FP64 otherwise);
+* otherwise by a pass over P, F and the pending kicks that writes nothing.
 
 After every boost the reported energy must equal 1/2 sum P^2/m of the momenta
 downloaded at that point (which applies the pending kicks), and a step sequence
@@ -85,7 +86,7 @@ def test_boost_energies_varying_kicks(gpu):
         ke = ke_of(gpu, md, N, m)
         assert abs(md.Kinetic.Total - ke.sum()) <= 1e-13 * ke.sum()
     gpu.EmDee_displace(C.byref(md), 1.0, 0.0, 0.004)
-    gpu.EmDee_boost(C.byref(md), 1.0, 0.0, 0.003)   # forces recomputed: the pair epilogue
+    gpu.EmDee_boost(C.byref(md), 1.0, 0.0, 0.003)   # forces recomputed: the two-kick pass
     k1 = md.Kinetic.Total
     gpu.EmDee_boost(C.byref(md), 1.0, 0.0, 0.002)   # a different kick: no speculative value
     k2 = md.Kinetic.Total
