@@ -154,12 +154,12 @@ def fp32_peak_tflops(torch):
     return best
 
 
-def read_traffic(name="pair_lj1m_traffic.txt"):
-    """DRAM bytes per kernel launch from a committed ncu summary, if any."""
+def read_traffic(name="pair_lj1m_traffic.txt", key="dram_bytes_per_launch"):
+    """A per-launch figure (DRAM bytes by default) from a committed ncu summary, if any."""
     p = os.path.join(ROOT, "profiles", name)
     try:
         for line in open(p):
-            if line.startswith("dram_bytes_per_launch"):
+            if line.startswith(key):
                 return float(line.split()[1])
     except OSError:
         pass
@@ -318,6 +318,15 @@ def run_gpu(args):
                 "peak_theoretical": fp32_theory, "frac_theoretical": achieved / fp32_theory,
                 "flops_per_launch": flops, "half_list_pairs": listed.value, "pairs_within_rc": within.value,
                 "us_per_launch": pair_s * 1e6}
+    # the pair kernel's binding unit: the SM's shared-memory pipe, one wavefront per clock
+    # per SM (wavefronts per launch from the committed ncu capture, ~55 % of them
+    # bank-conflict replays of the position gathers)
+    waves = read_traffic(key="shared_wavefronts_per_launch")
+    smem_peak = 152 * (clk.get("sm_max_mhz") or 2070.0) * 1e6
+    roofline_smem = None if waves is None else {
+        "bound": "shared-memory pipe", "kernel": "k_pair_mixed (pair forces)",
+        "achieved": waves / pair_s, "peak": smem_peak, "unit": "wavefronts/s", "frac": waves / pair_s / smem_peak,
+        "wavefronts_per_launch": waves, "source": "profiles/pair_lj1m_traffic.txt (ncu) / CUDA-event launch time"}
     boost_bytes = 72.0 * N   # P read+write, F read (steps with energies only)
     # fused step (two deferred kicks + move + skin displacement + FP32 packing), unit masses:
     # P r/w 48, F 24, R r/w 48, R0 24, build-time position and charge 16, slot 4, packed position 16
@@ -391,7 +400,7 @@ def run_gpu(args):
                 "config": workload_config(W, world=world), "neighbor_builds_in_timed_region": builds,
                 "tile_edge_cells": lib.EmDee_tile_edge(md),
                 "block_threads": {"build": lib.EmDee_tile_threads(md, 0), "pair": lib.EmDee_tile_threads(md, 1)},
-                "clocks": clk, "gpu_launches": int(launches), "roofline": roofline, "roofline_hbm": roofline_hbm,
+                "clocks": clk, "gpu_launches": int(launches), "roofline": roofline, "roofline_smem": roofline_smem, "roofline_hbm": roofline_hbm,
                 "roofline_step": roofline_step,
                 "kernels": per_kernel, "e2e": e2e, "cpu_baseline": cpu, "workloads": extra}
         print(json.dumps(line))
