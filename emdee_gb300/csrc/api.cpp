@@ -1220,7 +1220,9 @@ void EmDee_boost(tEmDee* md, double lambda, double alpha, double dt) {
       for (int d = 0; d < 3; d++) twoKE[d] = s.keSpec[d];
     } else {
       if (stale) compute_forces_impl(md);   // applies the pending kicks first
-      if (stale && s.npend == 0) {
+      // no kick pending (new forces, or momenta just uploaded): the two-kick pass, whose
+      // second sum also serves an identical boost that follows
+      if (s.npend == 0) {
         device_kinetic_two(s, CF);
         for (int d = 0; d < 3; d++) {
           twoKE[d] = s.hResult[48 + d];
