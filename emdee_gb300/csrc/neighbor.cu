@@ -752,8 +752,9 @@ static int choose_tile(const System& s, int M, double perCell) {
 // cells (the rule's edge always among them) a first build sizes the tiles; then the
 // list build and the pair kernel are timed with CUDA events (the faster of two
 // launches, after a warm-up launch of the pair kernel), each after a pass that moves
-// the memory traffic of an integration step, at the rule's block size and at every block size that gives each thread the same
-// number of the tile's atoms (1 to 4 rounds, 64 to 512 threads).  The cost of an
+// the memory traffic of an integration step, at the rule's block size and at every
+// block size that gives each thread the same number of the tile's atoms (1 to 4
+// rounds, 64 to 512 threads).  The cost of an
 // edge is its fastest pair launch plus a seventh of its fastest build (a rebuild
 // every ~7 steps, typical of a liquid with the reference's skin).  The rule's edge
 // and block sizes stay unless another choice is more than 5 % cheaper.  The choice
