@@ -894,7 +894,15 @@ void EmDee_upload(tEmDee* md, char* option, double* address) {
     if (s.hMirrorP) memcpy(s.hMirrorP, address, sizeof(double) * n3);
     double t2[3] = {0, 0, 0}, r2[3] = {0, 0, 0};   // src/EmDeeData.f90:157-189
     if (s.nbodies == 0) {
-      device_kinetic(s, t2, src);   // every atom is free: sum on the device
+      // every atom is free: sum on the device, and with FP32-exact forces in place the
+      // sums of the boost a velocity-Verlet step would do next (its speculative value)
+      const bool spec = s.precision == 0 && s.forcesF32 && s.forcesUpToDate[s.layer - 1] && s.haveLastBoostCF &&
+                        !s.phaseShared && !mirrors_active(s);
+      if (device_kinetic(s, t2, src, spec ? &s.lastBoostCF : nullptr)) {
+        for (int d = 0; d < 3; d++) s.keSpec[d] = s.hResult[56 + d];
+        s.keSpecCF = s.lastBoostCF;
+        s.keSpecValid = true;
+      }
     } else {
       for (int i : s.freeList)
         for (int d = 0; d < 3; d++) t2[d] += s.invMass[i] * (address[3 * i + d] * address[3 * i + d]);
@@ -1211,6 +1219,8 @@ void EmDee_boost(tEmDee* md, double lambda, double alpha, double dt) {
   // scattered momentum loads and the extra registers cost the pair kernel 31 us at 1M
   // atoms against 23.5 us for this pass.)
   if (compute && deferrable && s.precision == 0) {
+    s.lastBoostCF = CF;
+    s.haveLastBoostCF = true;
     double twoKE[3];
     const bool stale = lambda != 0.0 && !s.forcesUpToDate[s.layer - 1];
     const bool spec = s.keSpecValid && !stale && s.keSpecCF == CF;

@@ -72,22 +72,42 @@ static int motion_blocks(int N) {
 // reductions and the block partials few.
 // COPY: the momenta come from src (the caller's pinned host buffer, read over the
 // host link) and are stored into P on the way.
-template <bool UNITM, bool COPY>
+// SPEC (unit masses, FP32-exact forces F): also 2KE per dimension of P + cf F in
+// float-float arithmetic, the kinetic sums of an identical boost that follows (the
+// first half-kick of a velocity-Verlet step), into result[56..58]; the F reads ride
+// along with the slower reads of src.
+template <bool UNITM, bool COPY, bool SPEC>
 __global__ void __launch_bounds__(MOTION_THREADS) k_kinetic(const double* __restrict__ src, double* __restrict__ P,
                                                             const double* __restrict__ invMass, int N,
                                                             double* partials, unsigned int* ticket, double* result,
-                                                            double* hostResult) {
+                                                            double* hostResult, const double* __restrict__ F,
+                                                            float cfh, float cfl, unsigned int* specTicket) {
   const size_t n3 = 3 * (size_t)N, stride = (size_t)gridDim.x * blockDim.x;
   const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   double k = 0.0;
+  float sh = 0.f, sl = 0.f;
   for (size_t j = g; j < n3; j += stride) {
     const double p = src[j];
     if (COPY) P[j] = p;
     k += UNITM ? p * p : invMass[j / 3] * (p * p);
+    if (SPEC) {
+      const float f = ffk_round(F[j]);
+      float ph, pl, h, l;
+      ffk_split(p, ph, pl);
+      const float q = __fmul_rn(cfh, f), qe = fmaf(cfl, f, fmaf(cfh, f, -q));
+      ffk_add(ph, pl, q, qe, h, l);
+      ffk_sq_acc(h, l, sh, sl);
+    }
   }
   const int d = (int)(g % 3);
   double k2[3] = {d == 0 ? k : 0.0, d == 1 ? k : 0.0, d == 2 ? k : 0.0};
   grid_reduce<3, MOTION_THREADS>(k2, partials, ticket, result + 10, hostResult + 10);
+  if (SPEC) {
+    const float vh[3] = {d == 0 ? sh : 0.f, d == 1 ? sh : 0.f, d == 2 ? sh : 0.f};
+    const float vl[3] = {d == 0 ? sl : 0.f, d == 1 ? sl : 0.f, d == 2 ? sl : 0.f};
+    grid_reduce_ff2<3, MOTION_THREADS>(vh, vl, reinterpret_cast<float2*>(partials + 3 * gridDim.x), specTicket,
+                                       result + 56, hostResult + 56);
+  }
 }
 
 template <bool FMA>
@@ -174,23 +194,27 @@ void device_kick_out(System& s, double* out) {
   CK(cudaStreamSynchronize(s.stream));
 }
 
-void device_kinetic(System& s, double* twoKE, const double* src) {
+bool device_kinetic(System& s, double* twoKE, const double* src, const double* specCF) {
   const int N = s.natoms;
   // a multiple of 3 blocks (the grid stride over P[3N] must be), at most 3 per SM
   const int blocks = std::min(3 * ((N + 3 * MOTION_THREADS - 1) / (3 * MOTION_THREADS)), 3 * 152);
-  if (s.keCap < blocks) {
+  if (s.keCap < 2 * blocks) {   // FP64 partials, then the float-float ones of SPEC
     CK(cudaFree(s.dKE));
-    s.keCap = blocks;
-    CK(cudaMalloc(&s.dKE, sizeof(double) * 3 * blocks));
+    s.keCap = 2 * blocks;
+    CK(cudaMalloc(&s.dKE, sizeof(double) * 3 * s.keCap));
   }
-  auto kern = src ? (s.unitMass ? k_kinetic<true, true> : k_kinetic<false, true>)
-                 : (s.unitMass ? k_kinetic<true, false> : k_kinetic<false, false>);
+  const bool spec = specCF != nullptr && s.unitMass;
+  const float ch = spec ? (float)*specCF : 0.f, cl = spec ? (float)(*specCF - (double)ch) : 0.f;
+  auto kern = spec ? (src ? k_kinetic<true, true, true> : k_kinetic<true, false, true>)
+              : src ? (s.unitMass ? k_kinetic<true, true, false> : k_kinetic<false, true, false>)
+                    : (s.unitMass ? k_kinetic<true, false, false> : k_kinetic<false, false, false>);
   // the last block writes the sums into the pinned hResult as well: no copy back
   kern<<<blocks, MOTION_THREADS, 0, s.stream>>>(src ? src : s.dP, s.dP, s.dInvMass, N, s.dKE, s.dTicket + 1,
-                                                s.dResult, s.hResult);
+                                                s.dResult, s.hResult, s.F(), ch, cl, s.dTicket + 8);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(s.stream));
   for (int d = 0; d < 3; d++) twoKE[d] = s.hResult[10 + d];
+  return spec;
 }
 
 // 2KE per dimension of P + cf[0] F + ... + cf[NK] F (the pending kicks and one more,

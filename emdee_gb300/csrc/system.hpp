@@ -248,6 +248,10 @@ struct System {
   int buildRounds = 0, pairRounds = 0;
   bool tileTuned = false;   // device_tune_tile has run for this system
   double keSpecCF = 0.0, keSpec[3] = {0.0, 0.0, 0.0};
+  // CF of the last deferred boost with energies: a momenta upload sums 2KE for an
+  // identical kick that follows (keSpec) while it reads the caller's array
+  bool haveLastBoostCF = false;
+  double lastBoostCF = 0.0;
   bool skinReady = false, packReady = false;
   bool phaseShared = false;   // R/P aliased with another system (no deferral then)
   const double* pairSkip = nullptr;   // device rebuild flag the mixed pair kernel checks first
@@ -340,7 +344,10 @@ void device_kinetic_two(System& s, double CF);
 // 2KE per dimension of the momenta, free atoms only (no bodies); src: the momenta are
 // read from there (a device-accessible pointer to the caller's pinned buffer) and
 // stored into P on the way
-void device_kinetic(System& s, double* twoKE, const double* src = nullptr);
+// 2KE per dimension of the momenta (read from src, a pinned host buffer, and stored
+// into P when given).  With specCF (unit masses) it also sums 2KE of P + specCF F
+// into hResult[56..58] and returns true.
+bool device_kinetic(System& s, double* twoKE, const double* src = nullptr, const double* specCF = nullptr);
 // applies the pending kicks (1 or 2) and writes the momenta to P and to out (a
 // device-accessible pointer to the caller's pinned buffer); synchronizes
 void device_kick_out(System& s, double* out);

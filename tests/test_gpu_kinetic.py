@@ -113,3 +113,31 @@ def test_kinetic_trajectory_vs_oracle(gpu, oracle):
         worst = max(worst, abs(b.Kinetic.Total / a.Kinetic.Total - 1))
     print("kinetic energy, worst relative difference over 30 steps: %.2e" % worst)
     assert worst < 1e-6
+
+
+@pytest.mark.parametrize("pinned", [False, True])
+def test_boost_energies_after_momenta_upload(gpu, pinned):
+    """A velocity-Verlet loop that uploads new momenta at the start of every step
+    (the upload also sums the kinetic energy of the next half-kick): each boost's
+    energy equals 1/2 sum P^2 of the momenta downloaded right after it."""
+    N, dt = 2048, 0.005
+    md, m = system(gpu, N, [1.0], MIXED)
+    md.Options.Compute = True
+    rng = np.random.default_rng(5)
+    if pinned:
+        torch = pytest.importorskip("torch")
+        buf = torch.empty((N, 3), dtype=torch.float64, pin_memory=True).numpy()
+    for step in range(8):
+        P = rng.normal(0.0, 1.2, (N, 3))
+        if pinned:
+            buf[:] = P
+            gpu.upload(md, "momenta", buf)
+        else:
+            gpu.upload(md, "momenta", np.ascontiguousarray(P))
+        for call in range(3):
+            if call == 1:
+                gpu.EmDee_displace(C.byref(md), 1.0, 0.0, dt)
+                continue
+            gpu.EmDee_boost(C.byref(md), 1.0, 0.0, 0.5 * dt)
+            ke = ke_of(gpu, md, N, m)
+            assert abs(md.Kinetic.Total - ke.sum()) <= 1e-13 * ke.sum(), (step, call)
