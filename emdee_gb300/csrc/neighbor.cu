@@ -718,7 +718,8 @@ static void grow(T*& p, size_t& have, size_t need) {
 
 
 int build_block_threads(const System& s) {
-  return tile_threads(s.grid.tileStride, s.buildRounds, s.buildRounds > 0 ? BUILD_THREADS : BUILD_THREADS_RULE);
+  return s.buildThreads > 0 ? std::min(s.buildThreads, BUILD_THREADS)
+                            : tile_threads(s.grid.tileStride, 0, BUILD_THREADS_RULE);
 }
 
 // the general build variant: several types, bodies, exclusions or layered lists
@@ -752,9 +753,9 @@ static int choose_tile(const System& s, int M, double perCell) {
 // cells (the rule's edge always among them) a first build sizes the tiles; then the
 // list build and the pair kernel are timed with CUDA events (the faster of two
 // launches, after a warm-up launch of the pair kernel), each after a pass that moves
-// the memory traffic of an integration step, at the rule's block size and at every
-// block size that gives each thread the same number of the tile's atoms (1 to 4
-// rounds, 64 to 512 threads).  The cost of an
+// the memory traffic of an integration step, at the rule's block size and at block
+// sizes from 64 to 512 threads (threads loop over the tile's atoms in rounds; the
+// best size balances the rounds of typical tiles against residency).  The cost of an
 // edge is its fastest pair launch plus a seventh of its fastest build (a rebuild
 // every ~7 steps, typical of a liquid with the reference's skin).  The rule's edge
 // and block sizes stay unless another choice is more than 5 % cheaper.  The choice
@@ -774,7 +775,7 @@ __global__ void k_touch(double* __restrict__ R, double* __restrict__ P, const do
 }
 
 struct TileChoice {
-  int tb, buildRounds, pairRounds;
+  int tb, buildThreads, pairThreads;
 };
 static std::vector<std::pair<std::vector<long>, TileChoice>> g_tileTuned;
 
@@ -789,8 +790,8 @@ void device_tune_tile(System& s, bool ljOnly, void (*pair)(System&)) {
   for (const auto& e : g_tileTuned)
     if (e.first == key) {
       s.tileOverride = e.second.tb;
-      s.buildRounds = e.second.buildRounds;
-      s.pairRounds = e.second.pairRounds;
+      s.buildThreads = e.second.buildThreads;
+      s.pairThreads = e.second.pairThreads;
       return;
     }
   const int rule = rule_tile(M, perCell);
@@ -815,22 +816,19 @@ void device_tune_tile(System& s, bool ljOnly, void (*pair)(System&)) {
   TileChoice choice = {rule, 0, 0};
   for (int tb = std::max(1, std::min(rule - 1, 3)); tb <= std::min(6, M); tb++) {
     s.tileOverride = tb;
-    s.buildRounds = s.pairRounds = 0;
+    s.buildThreads = s.pairThreads = 0;
     device_build_lists(s);   // sizes the tiles of this edge
     if (s.grid.TB != tb) continue;   // did not fit (halo or shared memory): the build shrank the edge
-    // rounds 0 (the rule) and the even splits with distinct block sizes
-    std::vector<int> rounds = {0}, sizes = {-1};
-    for (int r = 1; r <= 4; r++) {
-      const int th = tile_threads(s.grid.tileStride, r, 512);
-      if (th < 64 || (s.grid.tileStride + th - 1) / th != r) continue;
-      if (std::find(sizes.begin(), sizes.end(), th) != sizes.end()) continue;
-      rounds.push_back(r);
-      sizes.push_back(th);
-    }
+    // block sizes: 0 (the rule), then 64 to 256 threads in steps of 32 and 320 to 512
+    // in steps of 64, from the least the halo scans need up to the largest tile
+    const int thMin = halo_min_threads(make_geom(s.grid.M, tb)), thMax = (s.grid.tileStride + 31) / 32 * 32;
+    std::vector<int> sizes = {0};
+    for (int th = 64; th <= 512; th += th < 256 ? 32 : 64)
+      if (th >= thMin && th <= thMax) sizes.push_back(th);
     double msBuild = 1e30, msPair = 1e30, ruleBuild = 0.0, rulePair = 0.0;
     int rb = 0, rp = 0;
-    for (int r : rounds) {
-      s.buildRounds = r;
+    for (int r : sizes) {
+      s.buildThreads = r;
       const double ms = std::min(timed([&] { device_build_lists(s); }), timed([&] { device_build_lists(s); }));
       if (getenv("EMDEE_TUNE_LOG"))
         fprintf(stderr, "  edge %d build, %d threads: %.1f us\n", tb, build_block_threads(s), 1e3 * ms);
@@ -840,8 +838,8 @@ void device_tune_tile(System& s, bool ljOnly, void (*pair)(System&)) {
         rb = r;
       }
     }
-    for (int r : rounds) {
-      s.pairRounds = r;
+    for (int r : sizes) {
+      s.pairThreads = r;
       pair(s);   // warm-up
       const double ms = std::min(timed([&] { pair(s); }), timed([&] { pair(s); }));
       if (getenv("EMDEE_TUNE_LOG")) fprintf(stderr, "  edge %d pair, %d threads: %.1f us\n", tb, pair_block_threads(s), 1e3 * ms);
@@ -864,8 +862,8 @@ void device_tune_tile(System& s, bool ljOnly, void (*pair)(System&)) {
   CK(cudaEventDestroy(e0));
   CK(cudaEventDestroy(e1));
   s.tileOverride = choice.tb;
-  s.buildRounds = choice.buildRounds;
-  s.pairRounds = choice.pairRounds;
+  s.buildThreads = choice.buildThreads;
+  s.pairThreads = choice.pairThreads;
   s.r0Valid = false;   // the system's own first build comes next, with the chosen edge
   g_tileTuned.push_back({key, choice});
 }

@@ -365,7 +365,7 @@ static size_t pair_args(System& s, bool useInRc, double rc2scaled, bool general,
 }
 
 int pair_block_threads(const System& s) {
-  return tile_threads(s.grid.tileStride, s.pairRounds, s.pairRounds > 0 ? PAIR_THREADS : PAIR_THREADS_RULE);
+  return s.pairThreads > 0 ? std::min(s.pairThreads, PAIR_THREADS) : tile_threads(s.grid.tileStride, 0, PAIR_THREADS_RULE);
 }
 
 // variant: 0 single-type Lennard-Jones without charges, 1 general, 2 pair count only

@@ -243,9 +243,9 @@ struct System {
   bool keSpecValid = false;
   bool forcesF32 = false;   // the current layer's forces are exact FP32 values (mixed pair forces only)
   int tileOverride = 0;     // tile edge chosen by device_tune_tile (0: the rule)
-  // atoms per thread (rounds) of the list build and of the single-type pair kernel,
-  // chosen by device_tune_tile with the edge (0: the rule of tile_threads)
-  int buildRounds = 0, pairRounds = 0;
+  // threads per block of the list build and of the single-type pair kernel, chosen by
+  // device_tune_tile with the edge (0: the rule of tile_threads)
+  int buildThreads = 0, pairThreads = 0;
   bool tileTuned = false;   // device_tune_tile has run for this system
   double keSpecCF = 0.0, keSpec[3] = {0.0, 0.0, 0.0};
   // CF of the last deferred boost with energies: a momenta upload sums 2KE for an
