@@ -463,10 +463,12 @@ def measure_water(lib, pkg, torch, steps):
     stream = torch.cuda.ExternalStream(lib.EmDee_cuda_stream(md))
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("timed")
     e0.record(stream)
     vv(lib, md, W, steps, step0=5)
     e1.record(stream)
     e1.synchronize()
+    torch.cuda.nvtx.range_pop()
     ms = e0.elapsed_time(e1)
     out = {"metric": METRIC, "value": 12288 * steps / (ms * 1e-3), "unit": "atom-steps/s", "atoms": 12288,
            "steps": steps, "ms_per_step": ms / steps,
@@ -569,8 +571,9 @@ def measure_hmc(lib, torch, iterations, configs, epochs):
 
 def run_workload(args):
     """One secondary workload alone, one JSON line (no headline fields): the replica
-    batch (--replicas boxes, --replica-steps steps) or repeated surrogate force
-    evaluations of --chains chains of the 8000-atom binary mixture."""
+    batch (--replicas boxes, --replica-steps steps), the rigid water box (--water-steps
+    steps) or repeated surrogate force evaluations of --chains chains of the 8000-atom
+    binary mixture."""
     import torch
     from emdee_gb300.build import build
     build()
@@ -578,6 +581,8 @@ def run_workload(args):
     lib = emdee_gb300.load()
     if args.workload == "replicas":
         out = measure_replicas(lib, emdee_gb300, torch, args.replica_steps, args.replicas)
+    elif args.workload == "water":
+        out = measure_water(lib, emdee_gb300, torch, args.water_steps)
     else:
         from emdee_gb300.surrogate import Chains, Surrogate
         ch = Chains(lib, args.chains, 8000, 1000)
@@ -616,7 +621,7 @@ def main():
     ap.add_argument("--water-steps", type=int, default=500)
     ap.add_argument("--atoms", type=int, default=None,
                     help="smaller box of the same density (profiling runs); default 1,048,576")
-    ap.add_argument("--workload", default=None, choices=["replicas", "surrogate-forces"],
+    ap.add_argument("--workload", default=None, choices=["replicas", "surrogate-forces", "water"],
                     help="run one secondary workload alone and print its measurement (profiling runs)")
     ap.add_argument("--replicas", type=int, default=256, help="replica count of --workload replicas")
     ap.add_argument("--chains", type=int, default=8, help="chains of --workload surrogate-forces")
