@@ -109,7 +109,7 @@ def test_network_engines_agree(gpu):
     rg = ((a[3] - b[3]).norm() / a[3].norm()).item()
     rf = ((a[1] - b[1]).norm() / a[1].norm()).item()
     print("tcgen05 vs mma.sync: atom energies max %.2e, dE/dG rel %.2e, forces rel %.2e" % (ea, rg, rf))
-    assert ea < 2e-3 and rg < 5e-3 and rf < 5e-3
+    assert ea < 1e-4 and rg < 1e-4 and rf < 1e-4   # the same BF16 products, summed in another order
     m.close()
 
 
@@ -192,12 +192,13 @@ def test_training_gradient(gpu, so):
     oE, oF, ref = so.loss_gradient(R.cpu(), ch.L, torch.tensor(ch.types - 1), torch.tensor(p, dtype=torch.float64),
                                    DESC["rc"], DESC["mu0"], DESC["mu15"], DESC["width"], Et.cpu(), Ft.cpu(), 1.0, 1.0)
     print("loss (GPU, reference):", lE, lF, oE, oF)
-    assert abs(lE - oE) <= 0.05 * oE and abs(lF - oF) <= 0.05 * oF
+    # BF16 operands on the tensor cores against FP64: observed 6e-4 (energy) and 5e-6 (force)
+    assert abs(lE - oE) <= 5e-3 * oE and abs(lF - oF) <= 1e-4 * oF
     g = grad.cpu().double()
     cos = float((g * ref).sum() / (g.norm() * ref.norm()))
     ratio = float(g.norm() / ref.norm())
     print("gradient cosine %.5f, norm ratio %.4f" % (cos, ratio))
-    assert cos > 0.99 and 0.95 < ratio < 1.05
+    assert cos > 0.9995 and 0.995 < ratio < 1.005
     m.close()
     ch.close()
 
