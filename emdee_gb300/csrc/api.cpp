@@ -1229,11 +1229,18 @@ void EmDee_boost(tEmDee* md, double lambda, double alpha, double dt) {
     if (spec) {
       for (int d = 0; d < 3; d++) twoKE[d] = s.keSpec[d];
     } else {
-      if (stale) compute_forces_impl(md);   // applies the pending kicks first
+      if (stale) {   // applies the pending kicks first; the pair launch may queue the pass below
+        s.keChainReq = true;
+        s.keChainCF = CF;
+        s.keChained = false;
+        compute_forces_impl(md);
+        s.keChainReq = false;
+      }
       // no kick pending (new forces, or momenta just uploaded): the two-kick pass, whose
       // second sum also serves an identical boost that follows
       if (s.npend == 0) {
-        device_kinetic_two(s, CF);
+        if (!(stale && s.keChained)) device_kinetic_two(s, CF);
+        s.keChained = false;
         for (int d = 0; d < 3; d++) {
           twoKE[d] = s.hResult[48 + d];
           s.keSpec[d] = s.hResult[51 + d];

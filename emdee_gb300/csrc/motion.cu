@@ -275,7 +275,8 @@ __global__ void __launch_bounds__(MOTION_THREADS) k_kinetic_two(const double* __
                                                                 const double* __restrict__ F,
                                                                 const double* __restrict__ invMass, int N, double cf,
                                                                 double* partials, unsigned int* ticket, double* result,
-                                                                double* hostResult) {
+                                                                double* hostResult, const double* skip) {
+  if (skip != nullptr && __double_as_longlong(*skip) != 0) return;   // a rebuild is due: nothing to sum
   const size_t n3 = 3 * (size_t)N, stride = (size_t)gridDim.x * blockDim.x;
   const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   double k1 = 0.0, k2 = 0.0;
@@ -303,7 +304,9 @@ constexpr int KE_FF_LOADS = 4;
 __global__ void __launch_bounds__(MOTION_THREADS) k_kinetic_two_ff(const double* __restrict__ P,
                                                                    const double* __restrict__ F, int N, float cfh,
                                                                    float cfl, float2* partials, unsigned int* ticket,
-                                                                   double* result, double* hostResult) {
+                                                                   double* result, double* hostResult,
+                                                                   const double* skip) {
+  if (skip != nullptr && __double_as_longlong(*skip) != 0) return;   // a rebuild is due: nothing to sum
   const size_t n3 = 3 * (size_t)N, stride = (size_t)gridDim.x * blockDim.x;
   const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   float a1h = 0.f, a1l = 0.f, a2h = 0.f, a2l = 0.f;
@@ -331,7 +334,9 @@ __global__ void __launch_bounds__(MOTION_THREADS) k_kinetic_two_ff(const double*
   grid_reduce_ff2<6, MOTION_THREADS>(vh, vl, partials, ticket, result + 48, hostResult + 48);
 }
 
-void device_kinetic_two(System& s, double CF) {
+// skip: a device flag (0.0 or 1.0, tested on its bits) that makes the pass return at
+// once; the pass is queued without waiting for it
+static void launch_kinetic_two(System& s, double CF, const double* skip) {
   const int N = s.natoms;
   const int blocks = std::min(3 * ((N + 3 * MOTION_THREADS - 1) / (3 * MOTION_THREADS)), 3 * 152);
   // the float-float pass is latency-bound: as many blocks as fit at once (five per
@@ -348,13 +353,17 @@ void device_kinetic_two(System& s, double CF) {
   if (s.unitMass && s.forcesF32 && !fp64Only) {
     const float ch = (float)CF, cl = (float)(CF - (double)ch);
     k_kinetic_two_ff<<<ffBlocks, MOTION_THREADS, 0, s.stream>>>(s.dP, s.F(), N, ch, cl, (float2*)s.dKE,
-                                                             s.dTicket + 1, s.dResult, s.hResult);
+                                                             s.dTicket + 1, s.dResult, s.hResult, skip);
   } else {
     (s.unitMass ? k_kinetic_two<true> : k_kinetic_two<false>)<<<blocks, MOTION_THREADS, 0, s.stream>>>(
-        s.dP, s.F(), s.dInvMass, N, CF, s.dKE, s.dTicket + 1, s.dResult, s.hResult);
+        s.dP, s.F(), s.dInvMass, N, CF, s.dKE, s.dTicket + 1, s.dResult, s.hResult, skip);
   }
   CK(cudaGetLastError());
   prof_end(s, PK_BOOST);
+}
+
+void device_kinetic_two(System& s, double CF) {
+  launch_kinetic_two(s, CF, nullptr);
   CK(cudaStreamSynchronize(s.stream));
 }
 
@@ -397,6 +406,13 @@ bool device_pair_forces(System& s, bool compute, bool speculative) {
     s.pairSkip = nullptr;
   }
   prof_end(s, PK_PAIR);
+  // A boost that waits for these forces (free atoms, no bond, angle or k-space forces
+  // to be added to them) gets its kinetic sums from a pass queued right behind the
+  // pair kernel, which skips it too when a rebuild is due
+  const int l2 = s.layer - 1;
+  const bool chain = speculative && s.keChainReq && s.precision == 0 && s.nbodies == 0 &&
+                     s.bondedTerms.bonds.empty() && s.bondedTerms.angles.empty() && !s.coul[l2].requires_kspace;
+  if (chain) launch_kinetic_two(s, s.keChainCF, s.dResult + 9);
   // Mixed precision: the last block of the pair kernel wrote the sums, and the fused
   // step the skin value and rebuild flag ([8], [9]), straight into the pinned hResult,
   // so one synchronisation returns all of them.  FP64 mode copies them back.
@@ -405,9 +421,11 @@ bool device_pair_forces(System& s, bool compute, bool speculative) {
                        s.stream));
   CK(cudaStreamSynchronize(s.stream));
   if (speculative && s.hResult[9] != 0.0) {
+    if (chain) prof_drop_last(s);   // the kinetic pass returned at once as well
     prof_drop_last(s);
     return false;
   }
+  if (chain) s.keChained = true;
   return true;
 }
 

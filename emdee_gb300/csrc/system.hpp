@@ -252,6 +252,11 @@ struct System {
   // identical kick that follows (keSpec) while it reads the caller's array
   bool haveLastBoostCF = false;
   double lastBoostCF = 0.0;
+  // a deferred boost with energies that waits for new forces: the speculative pair
+  // launch queues the two-kick kinetic pass for kick keChainCF right behind it and
+  // sets keChained when that pass ran (no rebuild was due)
+  bool keChainReq = false, keChained = false;
+  double keChainCF = 0.0;
   bool skinReady = false, packReady = false;
   bool phaseShared = false;   // R/P aliased with another system (no deferral then)
   const double* pairSkip = nullptr;   // device rebuild flag the mixed pair kernel checks first
