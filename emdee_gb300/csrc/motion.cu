@@ -410,9 +410,9 @@ bool device_pair_forces(System& s, bool compute, bool speculative) {
   // to be added to them) gets its kinetic sums from a pass queued right behind the
   // pair kernel, which skips it too when a rebuild is due
   const int l2 = s.layer - 1;
-  const bool chain = speculative && s.keChainReq && s.precision == 0 && s.nbodies == 0 &&
-                     s.bondedTerms.bonds.empty() && s.bondedTerms.angles.empty() && !s.coul[l2].requires_kspace;
-  if (chain) launch_kinetic_two(s, s.keChainCF, s.dResult + 9);
+  const bool chain = s.keChainReq && s.precision == 0 && s.nbodies == 0 && s.bondedTerms.bonds.empty() &&
+                     s.bondedTerms.angles.empty() && !s.coul[l2].requires_kspace;
+  if (chain) launch_kinetic_two(s, s.keChainCF, speculative ? s.dResult + 9 : nullptr);
   // Mixed precision: the last block of the pair kernel wrote the sums, and the fused
   // step the skin value and rebuild flag ([8], [9]), straight into the pinned hResult,
   // so one synchronisation returns all of them.  FP64 mode copies them back.

@@ -795,6 +795,8 @@ void device_tune_tile(System& s, bool ljOnly, void (*pair)(System&)) {
       return;
     }
   const int rule = rule_tile(M, perCell);
+  const bool chainReq = s.keChainReq;   // no kinetic pass queued behind the timed pair launches
+  s.keChainReq = false;
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
@@ -865,6 +867,7 @@ void device_tune_tile(System& s, bool ljOnly, void (*pair)(System&)) {
   s.buildThreads = choice.buildThreads;
   s.pairThreads = choice.pairThreads;
   s.r0Valid = false;   // the system's own first build comes next, with the chosen edge
+  s.keChainReq = chainReq;
   g_tileTuned.push_back({key, choice});
 }
 
